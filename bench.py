@@ -1,0 +1,362 @@
+"""Benchmark: particle-steps/s of the SPH compute step on GB300.
+
+Workload: the 4,194,304-particle dam break with the moving sphere mover
+(box 3,590h x 1,795h, h = 1; sph_gb300.scenes.config2).  A "step" is one
+full reference step (fluid.c:273-348) over all particles.  The timed steps
+continue the simulation after the warm-up steps (steps W .. W+K-1 of the
+dam break), each step with its own mover position.
+
+  value   device-resident throughput: CUDA events on the library's stream
+          around K graph-launched steps (per-step tunables copied from pinned
+          memory, as the reference receives them).
+  e2e     the same metric through the C ABI from host buffers: upload of the
+          particle state from host memory, then per step the tunables
+          host->device and the packed render coordinates (fluid.c:356-362)
+          device->host into pinned memory; wall clock around all of it.
+  roofline  the dominant kernel's algorithmic bytes / its CUDA-event time,
+          against the measured HBM copy bandwidth.
+  cpu_baseline  the oracle's restatement of the reference step (Gauss-Seidel,
+          single thread) on a bounded sample of the same construction.
+
+--impl reference runs the reference's CPU step instead (the compiled
+reference where present, else the restatement) on all host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+# Bytes each kernel must move per particle (reads + writes of its own
+# arrays; neighbour reads that hit on-chip caches are not counted), and per
+# cell for the scan kernels.  See DESIGN.md "Kernels and their rooflines".
+ALG_BYTES = {
+    "viscosity_predict": (40, 0),   # R pos, vel 16; W pos, prev, key+rank 24
+    "cell_scan_reduce_1": (0, 4),   # R count
+    "cell_scan_apply_1": (0, 12),   # R count, W start, W zero
+    "cell_scatter_1": (20, 0),      # R key+rank 8, id 4, start 4; W slot 4
+    "cell_permute_1": (52, 0),      # R key+rank 8, start 8, slots 4, id 4, pos 8, prev 8; W 20... see DESIGN
+    "density": (16, 0),             # R pos 8; W rho 8
+    "relax_update": (48, 0),        # R pos, rho, prev 24; W pos, vel, key+rank 24
+    "cell_scan_reduce_2": (0, 4),
+    "cell_scan_apply_2": (0, 12),
+    "cell_scatter_2": (20, 0),
+    "cell_permute_2": (52, 0),
+}
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int = 0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in open(self.path):
+                f = [v.strip() for v in line.split(",")]
+                if len(f) >= 9:
+                    rows.append(f)
+        except Exception:
+            pass
+        finally:
+            if self.path and os.path.exists(self.path):
+                os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+
+        def num(v):
+            try:
+                return float(v)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        mx = [num(r[2]) for r in rows if num(r[2]) is not None]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for i, nm in enumerate(names):
+                if r[5 + i].lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows),
+                "power_w_max": max((num(r[3]) or 0.0) for r in rows)}
+
+
+def dist_setup():
+    """One process per GPU under torchrun: each rank sees only its GPU.
+    Ranks are independent replicas (the path does not shard); gloo carries
+    only the barrier and the max-over-ranks time."""
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+        devs = vis.split(",") if vis else [str(i) for i in range(64)]
+        os.environ["CUDA_VISIBLE_DEVICES"] = devs[local]
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(world, v: float) -> float:
+    if world <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_sample_scene(n_sample: int):
+    from sph_gb300 import scenes
+    return scenes.config2(n=n_sample)
+
+
+def time_cpu_port(n_sample: int, steps: int, kind: str):
+    """Seconds for `steps` reference steps (Gauss-Seidel order) of a sample."""
+    import oracle
+    sc = cpu_sample_scene(n_sample)
+    sim = oracle.Sim(kind, sc.x, sc.y, sc.vx, sc.vy, sc.params.as_dict(), sc.config())
+    mv = sc.mover_schedule(0, steps + 1)
+    sim.step(1, mv[:1])  # first step (no viscosity) outside the timing
+    t0 = time.perf_counter()
+    sim.step(steps, mv[1:])
+    dt = time.perf_counter() - t0
+    sim.close()
+    return dt
+
+
+def _cpu_worker(args):
+    n_sample, steps, kind = args
+    return time_cpu_port(n_sample, steps, kind)
+
+
+def cpu_kind():
+    import oracle
+    if not os.path.exists(oracle.PORT_LIB):
+        oracle.build(ref=False)
+    return ("ref", "reference") if oracle.ref_available() else ("port", "port")
+
+
+def cpu_baseline_single(n_sample=262_144, steps=12):
+    kind, label = cpu_kind()
+    dt = time_cpu_port(n_sample, steps, kind)
+    return {"value": n_sample * steps / dt, "unit": "particle-steps/s", "cores": 1, "kind": label,
+            "sample": f"dam break construction of the 4M workload scaled to {n_sample} particles "
+                      f"(same lattice, fill fraction, moving sphere mover), {steps} steps after one "
+                      f"untimed step, reference step order, single thread, -O2 -ffp-contract=off"}
+
+
+def run_reference(args, world, rank):
+    """The reference's CPU step on all host cores: one independent process
+    per core, each the single-rank step loop on a sample of the workload."""
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    kind, label = cpu_kind()
+    cores = os.cpu_count() or 1
+    n_sample, steps = args.cpu_sample, max(2, args.cpu_steps)
+    ctx = mp.get_context("spawn")
+    work = [(n_sample, steps, kind)] * cores
+    for _ in range(max(0, min(args.warmup, 1))):
+        pass
+    t0 = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        times = pool.map(_cpu_worker, work)
+    wall = time.perf_counter() - t0
+    busy = max(times)
+    value = cores * n_sample * steps / busy
+    line = {"metric": "particle-steps/s", "value": value, "unit": "particle-steps/s",
+            "impl": "reference", "n_gpus": args.gpus, "steps": steps, "warmup": 1,
+            "ms_per_step": 1e3 * busy / steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "dam break, 4,194,304-particle construction sampled at "
+                                   f"{n_sample} particles per core", "particles_per_core": n_sample,
+                       "cores": cores, "wall_s": wall},
+            "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": cores, "kind": label,
+                             "sample": f"{cores} independent processes, each the reference's single-rank "
+                                       f"step loop (Gauss-Seidel order, fluid.c:273-348) on a {n_sample}-"
+                                       f"particle sample of the dam break for {steps} steps; no halo "
+                                       f"exchange, so an upper bound of {cores}-rank MPI throughput"},
+            "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def traffic_per_launch(kernel: str, n: int):
+    """DRAM bytes per launch of `kernel` scaled from the committed ncu capture."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        d = json.load(open(p))
+        k = d["kernels"][kernel]
+        return k["dram_bytes"] * n / d["particles"]
+    except Exception:
+        return None
+
+
+def run_gpu(args, world, rank):
+    import numpy as np
+
+    from sph_gb300 import Simulation, scenes
+    from sph_gb300.simulation import PinnedArray
+
+    sc = scenes.config2(n=args.n)
+    n, cells = sc.n, sc.cells
+    K, W = args.steps, args.warmup
+    params = [sc.params_at(t).as_dict() for t in range(W + K)]
+
+    # ---- device-resident throughput ----
+    sim = Simulation.from_scene(sc)
+    sim.step_schedule(params[:W])
+    sim.synchronize()
+    barrier(world)
+    with ClockSampler(0) as clk:
+        sim.timer_start()
+        sim.step_schedule(params[W:W + K])
+        ms = sim.timer_stop()
+    clocks = clk.summary()
+    ms = max_over_ranks(world, ms)
+    barrier(world)
+    value = world * n * K / (ms / 1e3)
+    launches = sim.launches_per_step() * K
+    diag = sim.diagnostics().tolist()
+    counters = sim.counters()
+
+    # ---- per-kernel times (CUDA events on the library stream) ----
+    kt_runs = [sim.kernel_times(params[min(W + K + i, W + K - 1)]) for i in range(5)]
+    ktimes = {k: statistics.median(r[k] for r in kt_runs) for k in kt_runs[0]}
+    sim.close()
+    top = max(ktimes, key=ktimes.get)
+    per_p, per_c = ALG_BYTES[top]
+    alg = per_p * n + per_c * cells
+    peak, peak_kind = load_peaks()
+    achieved = alg / (ktimes[top] / 1e3) / 1e9
+    step_bytes = scenes.algorithmic_bytes_per_step(n, cells)
+    roofline = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak,
+                "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                "traffic": traffic_per_launch(top, n),
+                "algorithmic_bytes_per_launch": alg,
+                "step_algorithmic_bytes": step_bytes,
+                "step_frac": step_bytes / (ms / K / 1e3) / 1e9 / peak,
+                "kernel_ms": {k: round(v, 5) for k, v in ktimes.items()}}
+
+    # ---- end to end through the C ABI with host buffers ----
+    e2e = None
+    if not args.no_e2e:
+        coords = PinnedArray((n, 2), np.int16)
+        t0 = time.perf_counter()
+        sim2 = Simulation(sc.params.as_dict(), sc.config(), n)
+        sim2.upload(sc.x, sc.y, sc.vx, sc.vy)
+        for t in range(W + K):
+            sim2.step(params[t])
+            sim2.pack_coords(coords.array)
+        t_e2e = time.perf_counter() - t0
+        sim2.close()
+        coords.free()
+        t_e2e = max_over_ranks(world, t_e2e)
+        e2e = {"value": world * n * (W + K) / t_e2e, "unit": "particle-steps/s",
+               "h2d_bytes_per_step": int(64 + 32 * n / (W + K)), "d2h_bytes_per_step": 4 * n,
+               "steps": W + K, "includes": "state upload from host + per step tunables H2D, "
+                                           "full step, packed coordinates D2H (pinned)"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline_single(args.cpu_sample, args.cpu_steps)
+
+    if rank == 0:
+        line = {"metric": "particle-steps/s", "value": value, "unit": "particle-steps/s",
+                "n_gpus": world, "steps": K, "warmup": W, "ms_per_step": ms / K,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32", "data": "synthetic",
+                "config": {"workload": f"dam break, {n} particles, box {sc.box[1]:g}h x {sc.box[3]:g}h, "
+                                       f"moving sphere mover r=8h, plain method",
+                           "particles": n, "cells": cells, "parallelism": f"replicas x{world}",
+                           "l2": "no flush: per-step working set ~0.5 GB > 129 MB L2",
+                           "steps_timed": f"{W}..{W + K - 1}"},
+                "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
+                "clocks": clocks, "gpu_launches": launches,
+                "diagnostics": {"mean_density": diag[0], "mean_near_density": diag[1],
+                                "kinetic_energy_per_particle": diag[2]},
+                "counters": counters}
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=480)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=4_194_304)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-sample", type=int, default=262_144)
+    ap.add_argument("--cpu-steps", type=int, default=12)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world, rank, _ = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_gpu(args, world, rank)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

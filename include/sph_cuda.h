@@ -1,0 +1,210 @@
+/*
+ * sph_cuda.h -- libsph_cuda, device-resident fast API.
+ *
+ * A GB300 (sm_103a) implementation of one TinySPH compute rank's step
+ * (fluid.c:270-349): gravity, viscosity impulses, position prediction,
+ * uniform-grid neighbour build, double density relaxation with near
+ * density, box and mover collision, velocity update.  The particle state
+ * lives on the GPU in structure-of-arrays form, kept sorted by
+ * (grid cell, particle id); the host keeps the reference's structs.
+ *
+ * Replaces, for a single-device domain, the compute rank's loop body
+ * fluid.c:273-348 (with the MPI halo/migration calls of fluid.c:310-349
+ * gone: one domain, no neighbours).  The caller-side switch is shown in
+ * INTEGRATION.md.
+ *
+ * Conventions
+ *  - Every call returns an sph_status (0 = SPH_OK).  On failure
+ *    sph_cuda_last_error() returns a message (per host thread).
+ *  - A handle is used by one host thread at a time; different handles are
+ *    independent (no global state on this API).
+ *  - Work is queued on the handle's stream.  Calls that fill host buffers
+ *    (download, pack, lists, probes, diagnostics, counters) return only when
+ *    the data is in host memory; sph_cuda_step returns once queued.
+ *  - Particle "id" is the index in the caller's pointer array
+ *    (fluid_particle::id, fluid.h:69); outputs are indexed by id.
+ */
+#ifndef SPH_CUDA_H
+#define SPH_CUDA_H
+
+#include <stddef.h>
+
+#include "sph_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct sph_cuda sph_cuda_t;
+
+enum sph_status {
+    SPH_OK = 0,
+    SPH_ERR_INVALID = 1,     /* bad argument (null pointer, n out of range, bad grid) */
+    SPH_ERR_CUDA = 2,        /* a CUDA runtime call failed (message has the error) */
+    SPH_ERR_ALLOC = 3,       /* device or pinned-host allocation failed */
+    SPH_ERR_CAPACITY = 4,    /* n above the handle's capacity or output buffer too small */
+    SPH_ERR_STATE = 5,       /* e.g. step before upload */
+    SPH_ERR_UNSUPPORTED = 6  /* e.g. halo particles on a single-device domain */
+};
+
+/* Device-side event counters, accumulated since the last upload.  None of
+ * these events trap or stop the step; the reference drops the same cases
+ * silently (hash.c:160-165, 188, 223) or has undefined behaviour. */
+typedef struct sph_cuda_counters {
+    unsigned long long steps;          /* steps run since the last upload */
+    unsigned long long out_of_grid;    /* particle-builds whose cell key fell outside the
+                                          grid (negative/NaN coordinate or y == max_y;
+                                          undefined behaviour in hash.c:40-44): such a
+                                          particle gets no neighbours */
+    unsigned long long bucket_overflow;/* particle-builds beyond max_bucket_size in their
+                                          cell: dropped from the neighbour search, as
+                                          hash.c:160-165 drops them */
+    unsigned int max_cell_occupancy;   /* largest cell population seen */
+    unsigned int list_cap_risk;        /* nonzero if some half list could have exceeded
+                                          max_neighbors (hash.c:188, 223); the cap is not
+                                          reproduced, see the design doc */
+} sph_cuda_counters;
+
+/* Creates a handle for up to max_particles particles.
+ *   params:   tunable_params.smoothing_radius is h (fluid.c:159); the other
+ *             tunables are passed again to every step.
+ *   boundary: the global box (fluid.c:118-127); min_x/min_y should be 0 as in
+ *             the reference (fluid.c:117: "assumes in various spots min is 0").
+ *   grid:     spacing, size_x, size_y, max_bucket_size, max_neighbors as the
+ *             reference sets them (fluid.c:173-176, 214-215); its pointers are
+ *             ignored (the device owns its own cell lists).
+ * Replaces the host allocations of fluid.c:178-235. */
+int sph_cuda_create(sph_cuda_t **out, const param *params, const AABB_t *boundary,
+                    const neighbor_grid_t *grid, int max_particles);
+
+/* Frees all device and host resources of the handle. */
+int sph_cuda_destroy(sph_cuda_t *h);
+
+/* Queues subsequent work on `stream` (a cudaStream_t, NULL = the handle's own
+ * stream).  Re-captures the step graph. */
+int sph_cuda_set_stream(sph_cuda_t *h, void *stream);
+
+/* Uploads n particles (id = pointer-array index, fluid.c:197 / geometry.c:57)
+ * from the caller's pointer array and sorts them into cells.  Neighbour
+ * lists start empty, as after fluid.c:202's calloc: the first step after an
+ * upload has no viscosity impulses, exactly like the reference's first step.
+ * Replaces initParticles' hand-off (fluid.c:238). */
+int sph_cuda_upload(sph_cuda_t *h, fluid_particle *const *particle_pointers, int n);
+
+/* Same, from a contiguous array (particles[i] has id i). */
+int sph_cuda_upload_particles(sph_cuda_t *h, const fluid_particle *particles, int n);
+
+/* Same, from structure-of-arrays host buffers (x, y required; vx, vy may be NULL). */
+int sph_cuda_upload_soa(sph_cuda_t *h, const float *x, const float *y, const float *vx,
+                        const float *vy, int n);
+
+/* Runs nsteps steps with the given tunables (copied at call time).  Each step
+ * is the reference sequence fluid.c:273-348: apply_gravity,
+ * viscosity_impluses, predict_positions, hash_fluid(.., true),
+ * double_density_relaxation, updateVelocities, hash_fluid(.., false) --
+ * with viscosity and relaxation as deterministic gathers (Jacobi form).
+ * Captured as one CUDA graph per step. */
+int sph_cuda_step(sph_cuda_t *h, const tunable_parameters *tp, int nsteps);
+
+/* Runs nsteps steps, step t using tps[t] (e.g. a moving mover). */
+int sph_cuda_step_schedule(sph_cuda_t *h, const tunable_parameters *tps, int nsteps);
+
+/* Writes the particle state back through the caller's pointer array:
+ * x_prev, y_prev, x, y, v_x, v_y, density, density_near, pressure,
+ * pressure_near (a_x, a_y and id untouched).  Density and pressure are the
+ * values the last step's relaxation used (predicted positions), as in the
+ * reference's structs after a step. */
+int sph_cuda_download(sph_cuda_t *h, fluid_particle *const *particle_pointers, int n);
+
+/* Same, into a contiguous array indexed by id. */
+int sph_cuda_download_particles(sph_cuda_t *h, fluid_particle *particles, int n);
+
+/* Same, into structure-of-arrays host buffers (any pointer may be NULL). */
+int sph_cuda_download_soa(sph_cuda_t *h, float *x, float *y, float *vx, float *vy,
+                          float *density, float *density_near, int n);
+
+/* Packs the positions as pixel-space shorts for the render rank, by id:
+ * coords[2i] = (2 x/max_x - 1) * SHRT_MAX, coords[2i+1] likewise in y.
+ * Replaces the packing loop of fluid.c:356-362 (the MPI_Isend of fluid.c:364
+ * stays with the caller). */
+int sph_cuda_pack_coords_short(sph_cuda_t *h, short *coords, int n);
+
+/* Rebuilds the neighbour relation on the current positions, like
+ * hash_fluid(.., false) (fluid.c:341): after it, the next step applies
+ * viscosity impulses even if it is the first step after an upload. */
+int sph_cuda_rebuild_neighbors(sph_cuda_t *h);
+
+/* Waits for all queued work of the handle. */
+int sph_cuda_synchronize(sph_cuda_t *h);
+
+/* Copies the event counters out (synchronises). */
+int sph_cuda_get_counters(sph_cuda_t *h, sph_cuda_counters *out);
+
+/* FP64 diagnostics of the current state: out[0] mean density, out[1] mean
+ * near density (both from the last relaxation), out[2] kinetic energy per
+ * particle 0.5 |v|^2 (unit mass).  Deterministic reduction order. */
+int sph_cuda_diagnostics(sph_cuda_t *h, double out[3]);
+
+/* ---- parity probes: one pass on the CURRENT state, no state change ---- */
+
+/* The reference's half neighbour lists (hash_fluid, hash.c:127-242) on the
+ * current positions, in the reference's order: per particle (by id), the
+ * later particles of its own cell then the forward cells (0,+1), (+1,-1),
+ * (+1,0), (+1,+1), each cell in id order, cut at max_neighbors.
+ * counts[id] entries each, concatenated by id into ids (capacity max_total);
+ * *total receives the number of entries. */
+int sph_cuda_neighbor_lists(sph_cuda_t *h, int *counts, int *ids, long long max_total,
+                            long long *total);
+
+/* Density and near density of every particle on the current positions
+ * (hash_fluid(.., true) + calculate_density, hash.c:190-194 / fluid.c:527-539). */
+int sph_cuda_probe_density(sph_cuda_t *h, const tunable_parameters *tp, float *density,
+                           float *density_near);
+
+/* Relaxation displacement of every particle, treating the current positions
+ * as the predicted ones (density pass, then the gather form of
+ * double_density_relaxation, fluid.c:541-611), before boundary conditions. */
+int sph_cuda_probe_relaxation(sph_cuda_t *h, const tunable_parameters *tp, float *dx,
+                              float *dy);
+
+/* Viscosity velocity change of every particle on the current positions and
+ * velocities (gather form of viscosity_impluses, fluid.c:416-478). */
+int sph_cuda_probe_viscosity(sph_cuda_t *h, const tunable_parameters *tp, float *dvx,
+                             float *dvy);
+
+/* ---- measurement ---- */
+
+/* Runs ONE step (it advances the state) with a CUDA event pair around each
+ * kernel on the handle's stream.  ms[k] receives kernel k's time, *count the
+ * number of kernels (at most max); names via sph_cuda_kernel_name(k). */
+int sph_cuda_kernel_times(sph_cuda_t *h, const tunable_parameters *tp, float *ms, int max,
+                          int *count);
+const char *sph_cuda_kernel_name(int k);
+
+/* Kernels launched per step (graph nodes). */
+int sph_cuda_launches_per_step(sph_cuda_t *h);
+
+/* Device timer on the handle's stream: start records a CUDA event, stop
+ * records a second one, waits for it and returns the elapsed milliseconds. */
+int sph_cuda_timer_start(sph_cuda_t *h);
+int sph_cuda_timer_stop(sph_cuda_t *h, float *ms);
+
+/* Page-locked host memory for fast transfers (e.g. the packed coordinates
+ * buffer of sph_cuda_pack_coords_short), and its release. */
+int sph_cuda_host_alloc(void **ptr, size_t bytes);
+int sph_cuda_host_free(void *ptr);
+
+/* ---- misc ---- */
+
+/* Message of the last failed call on this host thread ("" if none). */
+const char *sph_cuda_last_error(void);
+
+/* sizeof of fluid_particle, neighbor, tunable_parameters, param, bucket_t,
+ * neighbor_grid_t, AABB_t as compiled into the library (7 ints). */
+int sph_cuda_abi_sizes(int *sizes, int n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPH_CUDA_H */

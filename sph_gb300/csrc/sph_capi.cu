@@ -1,0 +1,723 @@
+// sph_capi.cu -- handle lifecycle and the device-resident C API of libsph_cuda.
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+
+#include "sph_internal.h"
+
+namespace sph {
+
+// kernels.cu
+int launch_unpermute(sph_cuda *h, float2 *out);
+int launch_pack(sph_cuda *h, short2 *out);
+int launch_diagnostics(sph_cuda *h, double *d_out);
+int launch_probe(sph_cuda *h, int which, float2 *tmp_sorted, float2 *tmp_rho, float2 *out);
+int launch_half_lists(sph_cuda *h, unsigned *d_counts, int *d_off, int *d_ids, bool write);
+void enqueue_end_step(sph_cuda *h);
+const char *kernel_name(int k);
+int step_kernel_count();
+
+static thread_local char g_err[512] = "";
+
+void set_error(const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+}
+
+int cuda_fail(cudaError_t e, const char *what)
+{
+    if (e == cudaSuccess) return SPH_OK;
+    set_error("%s: %s (%s)", what, cudaGetErrorString(e), cudaGetErrorName(e));
+    return e == cudaErrorMemoryAllocation ? SPH_ERR_ALLOC : SPH_ERR_CUDA;
+}
+
+#define SPH_TRY(expr)                          \
+    do {                                       \
+        const int _rc = (expr);                \
+        if (_rc != SPH_OK) return _rc;         \
+    } while (0)
+#define SPH_CUDA(call) SPH_TRY(cuda_fail((call), #call))
+
+template <class T>
+static int dalloc(T **p, size_t count)
+{
+    *p = nullptr;
+    if (count == 0) count = 1;
+    return cuda_fail(cudaMalloc((void **)p, count * sizeof(T)), "cudaMalloc");
+}
+
+int ensure_scratch(sph_cuda *h, size_t bytes)
+{
+    if (bytes <= h->d_scratch_bytes) return SPH_OK;
+    if (h->d_scratch) cudaFree(h->d_scratch);
+    h->d_scratch = nullptr;
+    h->d_scratch_bytes = 0;
+    SPH_CUDA(cudaMalloc(&h->d_scratch, bytes));
+    h->d_scratch_bytes = bytes;
+    return SPH_OK;
+}
+
+int ensure_stage(sph_cuda *h, size_t bytes)
+{
+    if (bytes <= h->h_stage_bytes) return SPH_OK;
+    if (h->h_stage) cudaFreeHost(h->h_stage);
+    h->h_stage = nullptr;
+    h->h_stage_bytes = 0;
+    SPH_CUDA(cudaHostAlloc(&h->h_stage, bytes, cudaHostAllocDefault));
+    h->h_stage_bytes = bytes;
+    return SPH_OK;
+}
+
+static void destroy_graph(sph_cuda *h)
+{
+    if (h->exec) cudaGraphExecDestroy(h->exec);
+    if (h->graph) cudaGraphDestroy(h->graph);
+    h->exec = nullptr;
+    h->graph = nullptr;
+    h->graph_n = -1;
+}
+
+// One step as a graph (captured on the handle's stream).
+static int capture_step(sph_cuda *h)
+{
+    destroy_graph(h);
+    SPH_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    int nk = 0;
+    int rc = enqueue_step(h, nullptr, &nk);
+    enqueue_end_step(h);
+    cudaGraph_t g = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(h->stream, &g);
+    if (rc != SPH_OK) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    SPH_CUDA(ce);
+    h->graph = g;
+    SPH_CUDA(cudaGraphInstantiate(&h->exec, g, 0));
+    h->graph_n = h->n;
+    h->launches_per_step = nk + 1;
+    return SPH_OK;
+}
+
+// Copies the tunables into the device parameter block through a pinned
+// ring slot, so that the copy is asynchronous and the caller's struct can be
+// reused at once.  Skipped when unchanged.
+int set_params(sph_cuda *h, const tunable_parameters *tp)
+{
+    if (h->tp_valid && std::memcmp(&h->last_tp, tp, sizeof(*tp)) == 0) return SPH_OK;
+    const int s = h->params_next;
+    h->params_next = (s + 1) % h->params_ring;
+    SPH_CUDA(cudaEventSynchronize(h->params_ev[s]));
+    h->h_params_ring[s] = *tp;
+    SPH_CUDA(cudaMemcpyAsync(h->d_params, &h->h_params_ring[s], sizeof(*tp),
+                             cudaMemcpyHostToDevice, h->stream));
+    SPH_CUDA(cudaEventRecord(h->params_ev[s], h->stream));
+    h->last_tp = *tp;
+    h->tp_valid = true;
+    return SPH_OK;
+}
+
+int run_steps(sph_cuda *h, int nsteps)
+{
+    if (h->n == 0) return SPH_OK;
+    if (h->graph_n != h->n) SPH_TRY(capture_step(h));
+    for (int t = 0; t < nsteps; ++t) SPH_CUDA(cudaGraphLaunch(h->exec, h->stream));
+    return SPH_OK;
+}
+
+static int validate_tp(const tunable_parameters *tp)
+{
+    if (!tp) {
+        set_error("tunable parameters are NULL");
+        return SPH_ERR_INVALID;
+    }
+    if (!(tp->smoothing_radius > 0.0f) || !(tp->time_step > 0.0f)) {
+        set_error("smoothing_radius and time_step must be positive (got %g, %g)",
+                  (double)tp->smoothing_radius, (double)tp->time_step);
+        return SPH_ERR_INVALID;
+    }
+    return SPH_OK;
+}
+
+static int check_handle(sph_cuda *h)
+{
+    if (!h) {
+        set_error("null handle");
+        return SPH_ERR_INVALID;
+    }
+    return SPH_OK;
+}
+
+static int check_n(sph_cuda *h, int n)
+{
+    if (n < 0 || n > h->capacity) {
+        set_error("particle count %d outside [0, %d]", n, h->capacity);
+        return n < 0 ? SPH_ERR_INVALID : SPH_ERR_CAPACITY;
+    }
+    return SPH_OK;
+}
+
+// Host SoA (x, y, vx, vy, x_prev, y_prev, rho, rho_near) -> device, then sort.
+// `fill(i, rec)` writes particle i's 8 floats.
+template <class Fill>
+static int upload_common(sph_cuda *h, int n, Fill fill)
+{
+    SPH_TRY(check_n(h, n));
+    SPH_CUDA(cudaStreamSynchronize(h->stream));
+    SPH_TRY(ensure_stage(h, (size_t)n * 4 * sizeof(float2) + 16));
+    float2 *pos = (float2 *)h->h_stage, *vel = pos + n, *prev = vel + n, *rho = prev + n;
+    for (int i = 0; i < n; ++i) {
+        float r[8];
+        fill(i, r);
+        pos[i] = make_float2(r[0], r[1]);
+        vel[i] = make_float2(r[2], r[3]);
+        prev[i] = make_float2(r[4], r[5]);
+        rho[i] = make_float2(r[6], r[7]);
+    }
+    h->n = n;
+    const size_t b = (size_t)n * sizeof(float2);
+    if (n > 0) {
+        SPH_CUDA(cudaMemcpyAsync(h->pos_b, pos, b, cudaMemcpyHostToDevice, h->stream));
+        SPH_CUDA(cudaMemcpyAsync(h->vel_b, vel, b, cudaMemcpyHostToDevice, h->stream));
+        SPH_CUDA(cudaMemcpyAsync(h->prev_c, prev, b, cudaMemcpyHostToDevice, h->stream));
+        SPH_CUDA(cudaMemcpyAsync(h->rho_c, rho, b, cudaMemcpyHostToDevice, h->stream));
+    }
+    SPH_CUDA(cudaMemsetAsync(h->d_state, 0, sizeof(DevState), h->stream));
+    SPH_TRY(upload_soa_device(h, n));
+    SPH_CUDA(cudaStreamSynchronize(h->stream));  // staging buffer reuse
+    return SPH_OK;
+}
+
+// Sorted state -> id-order host SoA in the staging buffer (5 n float2:
+// pos, vel, prev, rho, pressure).  Synchronous.
+static int download_common(sph_cuda *h, int n, float2 **host)
+{
+    SPH_TRY(check_n(h, n));
+    if (n != h->n) {
+        set_error("download of %d particles, handle holds %d", n, h->n);
+        return SPH_ERR_INVALID;
+    }
+    const size_t b = (size_t)n * 5 * sizeof(float2);
+    SPH_TRY(ensure_scratch(h, b + 16));
+    SPH_TRY(ensure_stage(h, b + 16));
+    SPH_TRY(launch_unpermute(h, (float2 *)h->d_scratch));
+    if (n > 0)
+        SPH_CUDA(cudaMemcpyAsync(h->h_stage, h->d_scratch, b, cudaMemcpyDeviceToHost, h->stream));
+    SPH_CUDA(cudaStreamSynchronize(h->stream));
+    *host = (float2 *)h->h_stage;
+    return SPH_OK;
+}
+
+static void free_all(sph_cuda *h)
+{
+    destroy_graph(h);
+    void *ptrs[] = {h->pos_a, h->vel_a, h->id_a, h->pos_b, h->prev_b, h->vel_b, h->kr_b,
+                    h->pos_c, h->prev_c, h->rho_c, h->id_c, h->tmp_id, h->cnt, h->start_a,
+                    h->start_c, h->tile_sums, h->d_params, h->d_state, h->d_partials,
+                    h->d_scratch};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    if (h->h_stage) cudaFreeHost(h->h_stage);
+    if (h->h_params_ring) cudaFreeHost(h->h_params_ring);
+    if (h->params_ev) {
+        for (int i = 0; i < h->params_ring; ++i)
+            if (h->params_ev[i]) cudaEventDestroy(h->params_ev[i]);
+        delete[] h->params_ev;
+    }
+    for (cudaEvent_t e : h->timer)
+        if (e) cudaEventDestroy(e);
+    if (h->own_stream) cudaStreamDestroy(h->own_stream);
+}
+
+}  // namespace sph
+
+using namespace sph;
+
+extern "C" {
+
+const char *sph_cuda_last_error(void) { return sph::g_err; }
+
+int sph_cuda_create(sph_cuda_t **out, const param *params, const AABB_t *boundary,
+                    const neighbor_grid_t *grid, int max_particles)
+{
+    if (!out || !params || !boundary || !grid) {
+        set_error("sph_cuda_create: null argument");
+        return SPH_ERR_INVALID;
+    }
+    *out = nullptr;
+    if (max_particles < 0) {
+        set_error("max_particles %d < 0", max_particles);
+        return SPH_ERR_INVALID;
+    }
+    if (!(grid->spacing > 0.0f) || grid->size_x == 0 || grid->size_y == 0 ||
+        (unsigned long long)grid->size_x * grid->size_y >= (1ull << 30)) {
+        set_error("invalid neighbour grid (spacing %g, %u x %u)", (double)grid->spacing,
+                  grid->size_x, grid->size_y);
+        return SPH_ERR_INVALID;
+    }
+    if (grid->max_bucket_size == 0 || grid->max_neighbors == 0) {
+        set_error("max_bucket_size and max_neighbors must be positive");
+        return SPH_ERR_INVALID;
+    }
+    if (params->number_halo_particles != 0) {
+        set_error("halo particles (%d) are not supported: libsph_cuda runs a single-device domain",
+                  params->number_halo_particles);
+        return SPH_ERR_UNSUPPORTED;
+    }
+    SPH_TRY(validate_tp(&params->tunable_params));
+    sph_cuda *h = new (std::nothrow) sph_cuda();
+    if (!h) {
+        set_error("host allocation failed");
+        return SPH_ERR_ALLOC;
+    }
+    Grid &g = h->g;
+    g.spacing = grid->spacing;
+    g.size_x = (int)grid->size_x;
+    g.size_y = (int)grid->size_y;
+    g.ncells = g.size_x * g.size_y;
+    g.min_x = boundary->min_x;
+    g.max_x = boundary->max_x;
+    g.min_y = boundary->min_y;
+    g.max_y = boundary->max_y;
+    g.max_bucket = (int)grid->max_bucket_size;
+    g.max_neighbors = (int)grid->max_neighbors;
+    h->capacity = max_particles;
+
+    auto fail = [&](int rc) {
+        free_all(h);
+        delete h;
+        return rc;
+    };
+    int rc = cuda_fail(cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking),
+                       "cudaStreamCreate");
+    if (rc) return fail(rc);
+    h->stream = h->own_stream;
+    const size_t N = (size_t)max_particles;
+    const size_t C = (size_t)g.ncells;
+    const int scan_items = (int)((C + 1 > N ? C + 1 : N) + 1);
+    h->ntiles = (scan_items + kScanTile - 1) / kScanTile;
+    h->npartials = 148 * 2;
+    if ((rc = dalloc(&h->pos_a, N)) || (rc = dalloc(&h->vel_a, N)) || (rc = dalloc(&h->id_a, N)) ||
+        (rc = dalloc(&h->pos_b, N)) || (rc = dalloc(&h->prev_b, N)) ||
+        (rc = dalloc(&h->vel_b, N)) || (rc = dalloc(&h->kr_b, N)) || (rc = dalloc(&h->pos_c, N)) ||
+        (rc = dalloc(&h->prev_c, N)) || (rc = dalloc(&h->rho_c, N)) || (rc = dalloc(&h->id_c, N)) ||
+        (rc = dalloc(&h->tmp_id, N)) || (rc = dalloc(&h->cnt, C + 1 > N + 1 ? C + 1 : N + 1)) ||
+        (rc = dalloc(&h->start_a, C + 2 > N + 1 ? C + 2 : N + 1)) ||
+        (rc = dalloc(&h->start_c, C + 2)) || (rc = dalloc(&h->tile_sums, (size_t)h->ntiles)) ||
+        (rc = dalloc(&h->d_params, 1)) || (rc = dalloc(&h->d_state, 1)) ||
+        (rc = dalloc(&h->d_partials, (size_t)h->npartials * 3 + 3)))
+        return fail(rc);
+    rc = cuda_fail(cudaMemsetAsync(h->cnt, 0, (C + 1 > N + 1 ? C + 1 : N + 1) * sizeof(unsigned),
+                                   h->stream),
+                   "cudaMemset");
+    if (rc) return fail(rc);
+    rc = cuda_fail(cudaMemsetAsync(h->d_state, 0, sizeof(DevState), h->stream), "cudaMemset");
+    if (rc) return fail(rc);
+    h->params_ring = 64;
+    rc = cuda_fail(cudaHostAlloc((void **)&h->h_params_ring,
+                                 h->params_ring * sizeof(tunable_parameters), cudaHostAllocDefault),
+                   "cudaHostAlloc");
+    if (rc) return fail(rc);
+    h->params_ev = new (std::nothrow) cudaEvent_t[h->params_ring]();
+    if (!h->params_ev) return fail(SPH_ERR_ALLOC);
+    for (int i = 0; i < h->params_ring; ++i) {
+        rc = cuda_fail(cudaEventCreateWithFlags(&h->params_ev[i], cudaEventDisableTiming),
+                       "cudaEventCreate");
+        if (rc) return fail(rc);
+    }
+    for (cudaEvent_t &e : h->timer) {
+        rc = cuda_fail(cudaEventCreate(&e), "cudaEventCreate");
+        if (rc) return fail(rc);
+    }
+    rc = set_params(h, &params->tunable_params);
+    if (rc) return fail(rc);
+    rc = cuda_fail(cudaStreamSynchronize(h->stream), "create sync");
+    if (rc) return fail(rc);
+    *out = h;
+    return SPH_OK;
+}
+
+int sph_cuda_destroy(sph_cuda_t *h)
+{
+    if (!h) return SPH_OK;
+    cudaStreamSynchronize(h->stream);
+    free_all(h);
+    delete h;
+    return SPH_OK;
+}
+
+int sph_cuda_set_stream(sph_cuda_t *h, void *stream)
+{
+    SPH_TRY(check_handle(h));
+    SPH_CUDA(cudaStreamSynchronize(h->stream));
+    h->stream = stream ? (cudaStream_t)stream : h->own_stream;
+    destroy_graph(h);
+    return SPH_OK;
+}
+
+int sph_cuda_upload(sph_cuda_t *h, fluid_particle *const *ptrs, int n)
+{
+    SPH_TRY(check_handle(h));
+    if (!ptrs && n > 0) {
+        set_error("null particle pointer array");
+        return SPH_ERR_INVALID;
+    }
+    for (int i = 0; i < n; ++i)
+        if (!ptrs[i]) {
+            set_error("particle pointer %d is NULL", i);
+            return SPH_ERR_INVALID;
+        }
+    return upload_common(h, n, [&](int i, float *r) {
+        const fluid_particle *p = ptrs[i];
+        r[0] = p->x; r[1] = p->y; r[2] = p->v_x; r[3] = p->v_y;
+        r[4] = p->x_prev; r[5] = p->y_prev; r[6] = p->density; r[7] = p->density_near;
+    });
+}
+
+int sph_cuda_upload_particles(sph_cuda_t *h, const fluid_particle *ps, int n)
+{
+    SPH_TRY(check_handle(h));
+    if (!ps && n > 0) {
+        set_error("null particle array");
+        return SPH_ERR_INVALID;
+    }
+    return upload_common(h, n, [&](int i, float *r) {
+        const fluid_particle *p = &ps[i];
+        r[0] = p->x; r[1] = p->y; r[2] = p->v_x; r[3] = p->v_y;
+        r[4] = p->x_prev; r[5] = p->y_prev; r[6] = p->density; r[7] = p->density_near;
+    });
+}
+
+int sph_cuda_upload_soa(sph_cuda_t *h, const float *x, const float *y, const float *vx,
+                        const float *vy, int n)
+{
+    SPH_TRY(check_handle(h));
+    if ((!x || !y) && n > 0) {
+        set_error("x and y are required");
+        return SPH_ERR_INVALID;
+    }
+    return upload_common(h, n, [&](int i, float *r) {
+        r[0] = x[i]; r[1] = y[i]; r[2] = vx ? vx[i] : 0.0f; r[3] = vy ? vy[i] : 0.0f;
+        r[4] = x[i]; r[5] = y[i]; r[6] = 0.0f; r[7] = 0.0f;
+    });
+}
+
+int sph_cuda_step(sph_cuda_t *h, const tunable_parameters *tp, int nsteps)
+{
+    SPH_TRY(check_handle(h));
+    SPH_TRY(validate_tp(tp));
+    if (nsteps < 0) {
+        set_error("nsteps %d < 0", nsteps);
+        return SPH_ERR_INVALID;
+    }
+    SPH_TRY(set_params(h, tp));
+    return run_steps(h, nsteps);
+}
+
+int sph_cuda_step_schedule(sph_cuda_t *h, const tunable_parameters *tps, int nsteps)
+{
+    SPH_TRY(check_handle(h));
+    if (nsteps < 0 || (!tps && nsteps > 0)) {
+        set_error("bad schedule (%d steps)", nsteps);
+        return SPH_ERR_INVALID;
+    }
+    for (int t = 0; t < nsteps; ++t) {
+        SPH_TRY(validate_tp(&tps[t]));
+        SPH_TRY(set_params(h, &tps[t]));
+        SPH_TRY(run_steps(h, 1));
+    }
+    return SPH_OK;
+}
+
+int sph_cuda_download(sph_cuda_t *h, fluid_particle *const *ptrs, int n)
+{
+    SPH_TRY(check_handle(h));
+    if (!ptrs && n > 0) {
+        set_error("null particle pointer array");
+        return SPH_ERR_INVALID;
+    }
+    float2 *s = nullptr;
+    SPH_TRY(download_common(h, n, &s));
+    for (int i = 0; i < n; ++i) {
+        fluid_particle *p = ptrs[i];
+        if (!p) continue;
+        p->x = s[i].x; p->y = s[i].y;
+        p->v_x = s[n + i].x; p->v_y = s[n + i].y;
+        p->x_prev = s[2 * n + i].x; p->y_prev = s[2 * n + i].y;
+        p->density = s[3 * n + i].x; p->density_near = s[3 * n + i].y;
+        p->pressure = s[4 * n + i].x; p->pressure_near = s[4 * n + i].y;
+    }
+    return SPH_OK;
+}
+
+int sph_cuda_download_particles(sph_cuda_t *h, fluid_particle *ps, int n)
+{
+    SPH_TRY(check_handle(h));
+    if (!ps && n > 0) {
+        set_error("null particle array");
+        return SPH_ERR_INVALID;
+    }
+    float2 *s = nullptr;
+    SPH_TRY(download_common(h, n, &s));
+    for (int i = 0; i < n; ++i) {
+        fluid_particle *p = &ps[i];
+        p->x = s[i].x; p->y = s[i].y;
+        p->v_x = s[n + i].x; p->v_y = s[n + i].y;
+        p->x_prev = s[2 * n + i].x; p->y_prev = s[2 * n + i].y;
+        p->density = s[3 * n + i].x; p->density_near = s[3 * n + i].y;
+        p->pressure = s[4 * n + i].x; p->pressure_near = s[4 * n + i].y;
+    }
+    return SPH_OK;
+}
+
+int sph_cuda_download_soa(sph_cuda_t *h, float *x, float *y, float *vx, float *vy, float *rho,
+                          float *rho_near, int n)
+{
+    SPH_TRY(check_handle(h));
+    float2 *s = nullptr;
+    SPH_TRY(download_common(h, n, &s));
+    for (int i = 0; i < n; ++i) {
+        if (x) x[i] = s[i].x;
+        if (y) y[i] = s[i].y;
+        if (vx) vx[i] = s[n + i].x;
+        if (vy) vy[i] = s[n + i].y;
+        if (rho) rho[i] = s[3 * n + i].x;
+        if (rho_near) rho_near[i] = s[3 * n + i].y;
+    }
+    return SPH_OK;
+}
+
+int sph_cuda_pack_coords_short(sph_cuda_t *h, short *coords, int n)
+{
+    SPH_TRY(check_handle(h));
+    if (n != h->n || (!coords && n > 0)) {
+        set_error("pack: n %d (handle holds %d) or null buffer", n, h->n);
+        return SPH_ERR_INVALID;
+    }
+    const size_t b = (size_t)n * sizeof(short2);
+    SPH_TRY(ensure_scratch(h, b + 16));
+    SPH_TRY(launch_pack(h, (short2 *)h->d_scratch));
+    if (n > 0) SPH_CUDA(cudaMemcpyAsync(coords, h->d_scratch, b, cudaMemcpyDeviceToHost, h->stream));
+    SPH_CUDA(cudaStreamSynchronize(h->stream));
+    return SPH_OK;
+}
+
+int sph_cuda_rebuild_neighbors(sph_cuda_t *h)
+{
+    SPH_TRY(check_handle(h));
+    // The sorted state always carries the cell lists of its current
+    // positions, so the relation exists already: enable it.
+    const unsigned one = 1u;
+    SPH_CUDA(cudaMemcpyAsync(&h->d_state->lists_valid, &one, sizeof(one), cudaMemcpyHostToDevice,
+                             h->stream));
+    SPH_CUDA(cudaStreamSynchronize(h->stream));
+    return SPH_OK;
+}
+
+int sph_cuda_synchronize(sph_cuda_t *h)
+{
+    SPH_TRY(check_handle(h));
+    SPH_CUDA(cudaStreamSynchronize(h->stream));
+    return SPH_OK;
+}
+
+int sph_cuda_get_counters(sph_cuda_t *h, sph_cuda_counters *out)
+{
+    SPH_TRY(check_handle(h));
+    if (!out) {
+        set_error("null counters");
+        return SPH_ERR_INVALID;
+    }
+    DevState s;
+    SPH_CUDA(cudaMemcpyAsync(&s, h->d_state, sizeof(s), cudaMemcpyDeviceToHost, h->stream));
+    SPH_CUDA(cudaStreamSynchronize(h->stream));
+    out->steps = s.steps;
+    out->out_of_grid = s.out_of_grid;
+    out->bucket_overflow = s.bucket_overflow;
+    out->max_cell_occupancy = s.max_occ;
+    out->list_cap_risk = s.list_cap_risk;
+    return SPH_OK;
+}
+
+int sph_cuda_diagnostics(sph_cuda_t *h, double out[3])
+{
+    SPH_TRY(check_handle(h));
+    if (!out) {
+        set_error("null output");
+        return SPH_ERR_INVALID;
+    }
+    if (h->n == 0) {
+        out[0] = out[1] = out[2] = 0.0;
+        return SPH_OK;
+    }
+    double *d_out = h->d_partials + 3 * h->npartials;
+    SPH_TRY(launch_diagnostics(h, d_out));
+    SPH_CUDA(cudaMemcpyAsync(out, d_out, 3 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    SPH_CUDA(cudaStreamSynchronize(h->stream));
+    return SPH_OK;
+}
+
+int sph_cuda_neighbor_lists(sph_cuda_t *h, int *counts, int *ids, long long max_total,
+                            long long *total)
+{
+    SPH_TRY(check_handle(h));
+    if (!counts || !total) {
+        set_error("null output");
+        return SPH_ERR_INVALID;
+    }
+    const int n = h->n;
+    *total = 0;
+    if (n == 0) return SPH_OK;
+    // scratch: counts (n+1 words, scanned into offsets) | offsets (n+1) | ids
+    SPH_TRY(ensure_scratch(h, (size_t)(2 * n + 2) * sizeof(int) + 16));
+    unsigned *d_counts = (unsigned *)h->d_scratch;
+    int *d_off = (int *)(d_counts + n + 1);
+    SPH_CUDA(cudaMemsetAsync(d_counts, 0, (size_t)(n + 1) * sizeof(unsigned), h->stream));
+    SPH_TRY(launch_half_lists(h, d_counts, d_off, nullptr, false));
+    SPH_CUDA(cudaMemcpyAsync(counts, d_counts, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost,
+                             h->stream));
+    int tot = 0;
+    SPH_CUDA(cudaMemcpyAsync(&tot, d_off + n, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    SPH_CUDA(cudaStreamSynchronize(h->stream));
+    *total = tot;
+    if (tot > max_total || (!ids && tot > 0)) {
+        set_error("neighbour list buffer holds %lld entries, %d needed", max_total, tot);
+        return SPH_ERR_CAPACITY;
+    }
+    if (tot == 0) return SPH_OK;
+    // Counts were read before the scan zeroed nothing (zero_input = false).
+    int *d_ids = nullptr;
+    SPH_CUDA(cudaMallocAsync((void **)&d_ids, (size_t)tot * sizeof(int), h->stream));
+    int rc = launch_half_lists(h, nullptr, d_off, d_ids, true);
+    if (rc == SPH_OK)
+        rc = cuda_fail(cudaMemcpyAsync(ids, d_ids, (size_t)tot * sizeof(int),
+                                       cudaMemcpyDeviceToHost, h->stream),
+                       "list copy");
+    cudaFreeAsync(d_ids, h->stream);
+    if (rc == SPH_OK) rc = cuda_fail(cudaStreamSynchronize(h->stream), "list sync");
+    return rc;
+}
+
+static int probe(sph_cuda *h, const tunable_parameters *tp, int which, float *a, float *b)
+{
+    SPH_TRY(check_handle(h));
+    SPH_TRY(validate_tp(tp));
+    const int n = h->n;
+    if (n == 0) return SPH_OK;
+    if (!a || !b) {
+        set_error("null output");
+        return SPH_ERR_INVALID;
+    }
+    SPH_TRY(ensure_scratch(h, (size_t)n * 3 * sizeof(float2) + 16));
+    SPH_TRY(ensure_stage(h, (size_t)n * sizeof(float2) + 16));
+    float2 *t0 = (float2 *)h->d_scratch, *t1 = t0 + n, *out = t1 + n;
+    // probes use their own parameters without disturbing the step's
+    const tunable_parameters saved = h->last_tp;
+    const bool had = h->tp_valid;
+    SPH_TRY(set_params(h, tp));
+    SPH_TRY(launch_probe(h, which, t0, t1, out));
+    SPH_CUDA(cudaMemcpyAsync(h->h_stage, out, (size_t)n * sizeof(float2), cudaMemcpyDeviceToHost,
+                             h->stream));
+    if (had) SPH_TRY(set_params(h, &saved));
+    SPH_CUDA(cudaStreamSynchronize(h->stream));
+    const float2 *s = (const float2 *)h->h_stage;
+    for (int i = 0; i < n; ++i) {
+        a[i] = s[i].x;
+        b[i] = s[i].y;
+    }
+    return SPH_OK;
+}
+
+int sph_cuda_probe_density(sph_cuda_t *h, const tunable_parameters *tp, float *rho, float *rho_near)
+{
+    return probe(h, tp, 0, rho, rho_near);
+}
+
+int sph_cuda_probe_relaxation(sph_cuda_t *h, const tunable_parameters *tp, float *dx, float *dy)
+{
+    return probe(h, tp, 1, dx, dy);
+}
+
+int sph_cuda_probe_viscosity(sph_cuda_t *h, const tunable_parameters *tp, float *dvx, float *dvy)
+{
+    return probe(h, tp, 2, dvx, dvy);
+}
+
+int sph_cuda_kernel_times(sph_cuda_t *h, const tunable_parameters *tp, float *ms, int max,
+                          int *count)
+{
+    SPH_TRY(check_handle(h));
+    SPH_TRY(validate_tp(tp));
+    if (!ms || !count) {
+        set_error("null output");
+        return SPH_ERR_INVALID;
+    }
+    *count = 0;
+    if (h->n == 0) return SPH_OK;
+    SPH_TRY(set_params(h, tp));
+    cudaEvent_t ev[kMaxKernelsPerStep + 1];
+    const int ne = step_kernel_count() + 1;
+    for (int i = 0; i < ne; ++i) SPH_CUDA(cudaEventCreate(&ev[i]));
+    int nk = 0;
+    int rc = enqueue_step(h, ev, &nk);
+    enqueue_end_step(h);
+    if (rc == SPH_OK) rc = cuda_fail(cudaEventSynchronize(ev[nk]), "timing sync");
+    if (rc == SPH_OK) {
+        for (int k = 0; k < nk && k < max; ++k) cudaEventElapsedTime(&ms[k], ev[k], ev[k + 1]);
+        *count = nk < max ? nk : max;
+    }
+    for (int i = 0; i < ne; ++i) cudaEventDestroy(ev[i]);
+    return rc;
+}
+
+const char *sph_cuda_kernel_name(int k) { return sph::kernel_name(k); }
+
+int sph_cuda_launches_per_step(sph_cuda_t *h)
+{
+    if (!h) return 0;
+    return step_kernel_count() + 1;
+}
+
+int sph_cuda_timer_start(sph_cuda_t *h)
+{
+    SPH_TRY(check_handle(h));
+    SPH_CUDA(cudaEventRecord(h->timer[0], h->stream));
+    return SPH_OK;
+}
+
+int sph_cuda_timer_stop(sph_cuda_t *h, float *ms)
+{
+    SPH_TRY(check_handle(h));
+    if (!ms) {
+        set_error("null output");
+        return SPH_ERR_INVALID;
+    }
+    SPH_CUDA(cudaEventRecord(h->timer[1], h->stream));
+    SPH_CUDA(cudaEventSynchronize(h->timer[1]));
+    SPH_CUDA(cudaEventElapsedTime(ms, h->timer[0], h->timer[1]));
+    return SPH_OK;
+}
+
+int sph_cuda_host_alloc(void **ptr, size_t bytes)
+{
+    if (!ptr) {
+        set_error("null output");
+        return SPH_ERR_INVALID;
+    }
+    *ptr = nullptr;
+    SPH_CUDA(cudaHostAlloc(ptr, bytes ? bytes : 1, cudaHostAllocDefault));
+    return SPH_OK;
+}
+
+int sph_cuda_host_free(void *ptr)
+{
+    if (ptr) SPH_CUDA(cudaFreeHost(ptr));
+    return SPH_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,793 @@
+// sph_kernels.cu -- the step kernels of libsph_cuda (sm_103a).
+//
+// One step (fluid.c:273-348) is eleven kernels on one stream, captured as a
+// CUDA graph:
+//
+//   viscosity_predict   gravity + viscosity gather + predict + BCs + cell key   (A -> B)
+//   scan_reduce/apply   exclusive scan of the cell histogram -> cell starts      (C cells)
+//   scatter, permute    counting-sort scatter, then in-cell order by id          (B -> C)
+//   density             density / near-density gather                           (C)
+//   relax_update        relaxation gather + BCs + velocity update + cell key     (C -> B)
+//   scan_reduce/apply   cell starts of the relaxed positions                     (A cells)
+//   scatter, permute    back into (cell, id) order                              (B -> A)
+//
+// Every pass is a gather: a thread owns one particle (in sorted order) and
+// reads its 3x3 cell stencil, so no floating-point atomics exist and every
+// sum is taken in a fixed order: the results are deterministic.  The only
+// atomics are the integer cell-histogram increments, whose arrival rank is
+// used solely to give each particle a distinct scratch slot; the final
+// in-cell order is by id, recomputed deterministically in `permute`.
+#include <cstdio>
+
+#include "sph_device.cuh"
+
+namespace sph {
+
+// ---------------------------------------------------------------------------
+// block-wide helpers
+// ---------------------------------------------------------------------------
+
+template <class T>
+__device__ __forceinline__ T warp_sum(T v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ unsigned warp_max(unsigned v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Exclusive scan over the block; returns the thread's exclusive prefix and
+// the block total.  `sh` holds one word per warp.
+__device__ __forceinline__ unsigned block_exclusive_scan(unsigned v, unsigned *sh, unsigned &total)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    unsigned x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) sh[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned w = lane < nw ? sh[lane] : 0u;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < nw) sh[lane] = w;
+    }
+    __syncthreads();
+    total = sh[nw - 1];
+    const unsigned before = warp ? sh[warp - 1] : 0u;
+    __syncthreads();
+    return before + x - v;
+}
+
+// ---------------------------------------------------------------------------
+// cell build: histogram scan, scatter, permute
+// ---------------------------------------------------------------------------
+
+// Per-tile sums of the histogram (and occupancy statistics of the cells).
+__global__ void __launch_bounds__(kScanThreads)
+k_scan_reduce(const unsigned *__restrict__ in, int M, int ncells, int *__restrict__ tile_sums,
+              DevState *__restrict__ st, unsigned *occ, int max_bucket, int max_neighbors)
+{
+    __shared__ unsigned sh_s[kScanThreads / 32], sh_m[kScanThreads / 32];
+    __shared__ unsigned long long sh_e[kScanThreads / 32];
+    const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    unsigned s = 0, mx = 0;
+    unsigned long long excess = 0;
+    if (base + kScanItems <= M) {
+        const uint4 *p = reinterpret_cast<const uint4 *>(in + base);
+#pragma unroll
+        for (int q = 0; q < kScanItems / 4; ++q) {
+            const uint4 v = p[q];
+            const unsigned w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int idx = base + 4 * q + e;
+                s += w[e];
+                if (idx < ncells) {
+                    mx = max(mx, w[e]);
+                    if (w[e] > (unsigned)max_bucket) excess += w[e] - max_bucket;
+                }
+            }
+        }
+    } else {
+        for (int e = 0; e < kScanItems; ++e) {
+            const int idx = base + e;
+            const unsigned v = idx < M ? in[idx] : 0u;
+            s += v;
+            if (idx < ncells) {
+                mx = max(mx, v);
+                if (v > (unsigned)max_bucket) excess += v - max_bucket;
+            }
+        }
+    }
+    if (occ && ncells < M && base <= ncells && ncells < base + kScanItems)
+        atomicAdd(&st->out_of_grid, (unsigned long long)in[ncells]);
+    s = warp_sum(s);
+    mx = warp_max(mx);
+    excess = warp_sum(excess);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) { sh_s[warp] = s; sh_m[warp] = mx; sh_e[warp] = excess; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned ts = 0, tm = 0;
+        unsigned long long te = 0;
+        for (int w = 0; w < kScanThreads / 32; ++w) { ts += sh_s[w]; tm = max(tm, sh_m[w]); te += sh_e[w]; }
+        tile_sums[blockIdx.x] = (int)ts;
+        if (occ) {
+            atomicMax(occ, tm);
+            atomicMax(&st->max_occ, tm);
+            if (te) atomicAdd(&st->bucket_overflow, te);
+            const unsigned m = tm < (unsigned)max_bucket ? tm : (unsigned)max_bucket;
+            if (m > 0 && 5u * m - 1u > (unsigned)max_neighbors) atomicOr(&st->list_cap_risk, 1u);
+        }
+    }
+}
+
+// Exclusive scan: out[i] = sum(in[0..i)), out[M] = total.  Zeroes `in` when
+// asked (the histogram must be zero before the next build).
+__global__ void __launch_bounds__(kScanThreads)
+k_scan_apply(unsigned *__restrict__ in, int M, const int *__restrict__ tile_sums,
+             int *__restrict__ out, int zero_input)
+{
+    __shared__ unsigned sh[kScanThreads / 32];
+    __shared__ unsigned sh_prefix;
+    // prefix of all earlier tiles
+    unsigned acc = 0;
+    for (int t = threadIdx.x; t < (int)blockIdx.x; t += blockDim.x) acc += (unsigned)tile_sums[t];
+    acc = warp_sum(acc);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned p = 0;
+        for (int w = 0; w < kScanThreads / 32; ++w) p += sh[w];
+        sh_prefix = p;
+    }
+    __syncthreads();
+    const unsigned prefix = sh_prefix;
+    __syncthreads();
+
+    const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    unsigned v[kScanItems];
+    const bool full = base + kScanItems <= M;
+    if (full) {
+        const uint4 *p = reinterpret_cast<const uint4 *>(in + base);
+#pragma unroll
+        for (int q = 0; q < kScanItems / 4; ++q) {
+            const uint4 t = p[q];
+            v[4 * q] = t.x; v[4 * q + 1] = t.y; v[4 * q + 2] = t.z; v[4 * q + 3] = t.w;
+        }
+    } else {
+#pragma unroll
+        for (int e = 0; e < kScanItems; ++e) v[e] = base + e < M ? in[base + e] : 0u;
+    }
+    unsigned local = 0;
+#pragma unroll
+    for (int e = 0; e < kScanItems; ++e) local += v[e];
+    unsigned total;
+    unsigned run = prefix + block_exclusive_scan(local, sh, total);
+    if (full) {
+        int4 *o = reinterpret_cast<int4 *>(out + base);
+#pragma unroll
+        for (int q = 0; q < kScanItems / 4; ++q) {
+            int4 t;
+            t.x = (int)run; run += v[4 * q];
+            t.y = (int)run; run += v[4 * q + 1];
+            t.z = (int)run; run += v[4 * q + 2];
+            t.w = (int)run; run += v[4 * q + 3];
+            o[q] = t;
+        }
+        if (zero_input) {
+            uint4 *p = reinterpret_cast<uint4 *>(in + base);
+#pragma unroll
+            for (int q = 0; q < kScanItems / 4; ++q) p[q] = make_uint4(0, 0, 0, 0);
+        }
+    } else {
+#pragma unroll
+        for (int e = 0; e < kScanItems; ++e) {
+            if (base + e < M) {
+                out[base + e] = (int)run;
+                run += v[e];
+                if (zero_input) in[base + e] = 0u;
+            }
+        }
+    }
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == blockDim.x - 1) out[M] = (int)(prefix + total);
+}
+
+// Scratch slot per particle: cell start + arrival rank.
+__global__ void __launch_bounds__(kBlock)
+k_scatter_ids(int n, const uint2 *__restrict__ kr, const int *__restrict__ id_src,
+              const int *__restrict__ start, int *__restrict__ tmp)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint2 k = kr[i];
+    tmp[__ldg(start + k.x) + (int)k.y] = id_src ? id_src[i] : i;
+}
+
+// Final position = cell start + number of cell members with a smaller id, so
+// that each cell holds its particles in id order -- the order hash.c:153-163
+// inserts them into a bucket (pointer-array order).
+__global__ void __launch_bounds__(kBlock)
+k_permute(int n, const uint2 *__restrict__ kr, const int *__restrict__ start,
+          const int *__restrict__ tmp, const int *__restrict__ id_src,
+          const float2 *__restrict__ a_src, const float2 *__restrict__ b_src,
+          int *__restrict__ id_dst, float2 *__restrict__ a_dst, float2 *__restrict__ b_dst)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint2 k = kr[i];
+    const int s0 = __ldg(start + k.x), s1 = __ldg(start + k.x + 1);
+    const int myid = id_src ? id_src[i] : i;
+    int r;
+    if (s1 - s0 <= kRankScanMax) {
+        r = 0;
+        for (int j = s0; j < s1; ++j) r += __ldg(tmp + j) < myid;
+    } else {
+        r = (int)k.y;  // pathological cell: arrival order
+    }
+    const int d = s0 + r;
+    id_dst[d] = myid;
+    a_dst[d] = a_src[i];
+    if (b_src) b_dst[d] = b_src[i];
+}
+
+// Cell keys of uploaded positions (no step before them).
+__global__ void __launch_bounds__(kBlock)
+k_keys(int n, Grid g, const float2 *__restrict__ pos, uint2 *__restrict__ kr,
+       unsigned *__restrict__ cnt, unsigned *occ_reset)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0 && occ_reset) *occ_reset = 0u;
+    if (i >= n) return;
+    const float2 p = pos[i];
+    const unsigned key = cell_key(p.x, p.y, g);
+    kr[i] = make_uint2(key, atomicAdd(cnt + key, 1u));
+}
+
+// ---------------------------------------------------------------------------
+// pass 1: gravity + viscosity (gather) + predict + boundary + cell key
+// ---------------------------------------------------------------------------
+
+// apply_gravity (fluid.c:398-413), viscosity_impluses (fluid.c:416-478) in
+// gather form, predict_positions (fluid.c:507-523) with boundaryConditions.
+// Gather form of the viscosity: dv_i = -1/2 sum_j clamp5(I_ij),
+// I_ij = dt (1 - r/h)(sigma u + beta u^2) (x_j - x_i)/r for u > 0,
+// u = ((v_i - v_j).(x_j - x_i))/r, all from the velocities after gravity.
+// PROBE writes dv instead of advancing.
+template <bool PROBE>
+__global__ void __launch_bounds__(kBlock)
+k_viscosity_predict(int n, Grid g, const tunable_parameters *__restrict__ dP,
+                    DevState *__restrict__ st, const float2 *__restrict__ pos,
+                    const float2 *__restrict__ vel, const int *__restrict__ start,
+                    const unsigned *__restrict__ occ_in, unsigned *occ_reset,
+                    float2 *__restrict__ pos_out, float2 *__restrict__ prev_out,
+                    uint2 *__restrict__ kr_out, unsigned *__restrict__ cnt,
+                    float2 *__restrict__ probe_out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (!PROBE && i == 0) *occ_reset = 0u;
+    if (i >= n) return;
+    const tunable_parameters P = *dP;
+    const float dt = P.time_step;
+    const float gdt = __fmul_rn(-P.g, dt);
+    const float hh = P.smoothing_radius;
+    const float h2 = __fmul_rn(hh, hh);
+    const float h_recip = __fdiv_rn(1.0f, hh);
+    const float sigma = P.sigma, beta = P.beta;
+    const bool capped = *occ_in > (unsigned)g.max_bucket;
+
+    const float2 p = pos[i];
+    float2 v = vel[i];
+    v.y = __fadd_rn(v.y, gdt);
+    float dvx = 0.0f, dvy = 0.0f;
+    const unsigned key = cell_key(p.x, p.y, g);
+    if ((PROBE || st->lists_valid) && searchable(key, i, start, g, capped)) {
+        for_each_candidate(key, start, g, capped, [&](int j) {
+            if (j == i) return;
+            const float2 q = __ldg(pos + j);
+            const float qx = q.x - p.x, qy = q.y - p.y;
+            const float r2 = dist2(qx, qy);
+            if (r2 > h2 || r2 == 0.0f) return;
+            float2 w = __ldg(vel + j);
+            w.y = __fadd_rn(w.y, gdt);
+            const float r_recip = rsqrtf(r2);
+            const float r = r2 * r_recip;
+            const float u = ((v.x - w.x) * qx + (v.y - w.y) * qy) * r_recip;
+            if (u > 0.0f) {
+                const float ratio = r * h_recip;
+                const float imp = dt * (1.0f - ratio) * (sigma * u + beta * u * u);
+                dvx -= 0.5f * clamp5(imp * qx * r_recip);
+                dvy -= 0.5f * clamp5(imp * qy * r_recip);
+            }
+        });
+    }
+    if (PROBE) {
+        probe_out[i] = make_float2(dvx, dvy);
+        return;
+    }
+    v.x = __fadd_rn(v.x, dvx);
+    v.y = __fadd_rn(v.y, dvy);
+    float nx = __fadd_rn(p.x, __fmul_rn(v.x, dt));
+    float ny = __fadd_rn(p.y, __fmul_rn(v.y, dt));
+    boundary(nx, ny, P, g);
+    const unsigned k2 = cell_key(nx, ny, g);
+    const unsigned rank = atomicAdd(cnt + k2, 1u);
+    pos_out[i] = make_float2(nx, ny);
+    prev_out[i] = p;
+    kr_out[i] = make_uint2(k2, rank);
+}
+
+// ---------------------------------------------------------------------------
+// pass 2: density and near density (gather)
+// ---------------------------------------------------------------------------
+
+// rho_i = sum_j (1 - r/h)^2, rho_near_i = sum_j (1 - r/h)^3 over neighbours
+// j != i with r/h < 1 (calculate_density, fluid.c:527-539; the pairs of
+// hash_fluid, hash.c:185/221: r2 <= h2 inclusive).
+__global__ void __launch_bounds__(kBlock)
+k_density(int n, Grid g, const tunable_parameters *__restrict__ dP,
+          const float2 *__restrict__ pos, const int *__restrict__ start,
+          const unsigned *__restrict__ occ_in, float2 *__restrict__ rho_out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float hh = dP->smoothing_radius;
+    const float h2 = __fmul_rn(hh, hh);
+    const float h_recip = __fdiv_rn(1.0f, hh);
+    const bool capped = *occ_in > (unsigned)g.max_bucket;
+    const float2 p = pos[i];
+    const unsigned key = cell_key(p.x, p.y, g);
+    float a = 0.0f, b = 0.0f;
+    if (searchable(key, i, start, g, capped)) {
+        for_each_candidate(key, start, g, capped, [&](int j) {
+            if (j == i) return;
+            const float2 q = __ldg(pos + j);
+            const float r2 = dist2(p.x - q.x, p.y - q.y);
+            if (r2 > h2) return;
+            const float r = r2 > 0.0f ? r2 * rsqrtf(r2) : 0.0f;
+            const float ratio = __fmul_rn(r, h_recip);
+            if (ratio < 1.0f) {
+                const float omr = 1.0f - ratio;
+                const float omr2 = omr * omr;
+                a += omr2;
+                b += omr2 * omr;
+            }
+        });
+    }
+    rho_out[i] = make_float2(a, b);
+}
+
+// ---------------------------------------------------------------------------
+// pass 3: relaxation (gather) + boundary + velocity update + cell key
+// ---------------------------------------------------------------------------
+
+// Whether particle (slot i, id_i, cell ki) holds the pair with (slot j) in
+// its own half list in the reference: same cell and smaller id
+// (hash.c:178-199), or j's cell is one of i's forward cells
+// (0,+1), (+1,-1), (+1,0), (+1,+1) (hash.c:203-234).
+__device__ __noinline__ bool owns_pair(unsigned ki, int id_i, float2 qj, int id_j, const Grid &g)
+{
+    const unsigned kj = cell_key(qj.x, qj.y, g);
+    if (kj == ki) return id_i < id_j;
+    const int yi = (int)(ki / (unsigned)g.size_x), xi = (int)ki - yi * g.size_x;
+    const int yj = (int)(kj / (unsigned)g.size_x), xj = (int)kj - yj * g.size_x;
+    const int dx = xj - xi, dy = yj - yi;
+    return (dx == 0 && dy == 1) || (dx == 1 && dy >= -1 && dy <= 1);
+}
+
+// double_density_relaxation (fluid.c:541-611) in gather form:
+//   dx_i = sum_{j: 0 < r < h} D_ij (x_i - x_j)/r,
+//   D_ij = dt^2 [(P_i + P_j)(1 - r/h) + (Pn_i + Pn_j)(1 - r/h)^2 + k_spring (h - r)/2],
+//   P = k (rho - rest_density), Pn = k_near rho_near (fluid.c:560-565),
+// plus the reference's (1e-6, 1e-6) nudge for each pair with r <= 1e-6 that
+// the particle owns (fluid.c:583-586).  Then updateVelocities
+// (fluid.c:642-653): boundaryConditions, v = (x - x_prev)/dt clamped to +-5.
+// PROBE writes the displacement instead of advancing.
+template <bool PROBE>
+__global__ void __launch_bounds__(kBlock)
+k_relax_update(int n, Grid g, const tunable_parameters *__restrict__ dP,
+               const float2 *__restrict__ pos, const float2 *__restrict__ rho,
+               const float2 *__restrict__ prev, const int *__restrict__ ids,
+               const int *__restrict__ start, const unsigned *__restrict__ occ_in,
+               unsigned *occ_reset, float2 *__restrict__ pos_out, float2 *__restrict__ vel_out,
+               uint2 *__restrict__ kr_out, unsigned *__restrict__ cnt,
+               float2 *__restrict__ probe_out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (!PROBE && i == 0) *occ_reset = 0u;
+    if (i >= n) return;
+    const tunable_parameters P = *dP;
+    const float hh = P.smoothing_radius;
+    const float h2 = __fmul_rn(hh, hh);
+    const float h_recip = __fdiv_rn(1.0f, hh);
+    const float dt = P.time_step, dt2 = dt * dt;
+    const float k = P.k, k_near = P.k_near, rest = P.rest_density;
+    const float half_spring = 0.5f * P.k_spring;
+    const bool capped = *occ_in > (unsigned)g.max_bucket;
+
+    const float2 p = pos[i];
+    const float2 rp = rho[i];
+    const float Pi = k * (rp.x - rest), Pni = k_near * rp.y;
+    const unsigned key = cell_key(p.x, p.y, g);
+    float ax = 0.0f, ay = 0.0f;
+    int nudges = 0;
+    if (searchable(key, i, start, g, capped)) {
+        for_each_candidate(key, start, g, capped, [&](int j) {
+            if (j == i) return;
+            const float2 q = __ldg(pos + j);
+            const float ex = p.x - q.x, ey = p.y - q.y;
+            const float r2 = dist2(ex, ey);
+            if (r2 > h2) return;
+            if (r2 <= 1e-12f) {
+                // r <= 1e-6 (rare): the owner of the pair is nudged
+                const float r = r2 > 0.0f ? __fsqrt_rn(r2) : 0.0f;
+                if (r <= 0.000001f && owns_pair(key, ids[i], q, ids[j], g)) ++nudges;
+                if (!(r > 0.0f)) return;
+            }
+            const float r_recip = rsqrtf(r2);
+            const float r = r2 * r_recip;
+            const float ratio = r * h_recip;
+            if (ratio < 1.0f) {
+                const float2 rq = __ldg(rho + j);
+                const float omr = 1.0f - ratio;
+                const float D = dt2 * ((Pi + k * (rq.x - rest)) * omr +
+                                       (Pni + k_near * rq.y) * omr * omr +
+                                       half_spring * (hh - r));
+                const float s = D * r_recip;
+                ax += s * ex;
+                ay += s * ey;
+            }
+        });
+    }
+    const float nd = (float)nudges * 0.000001f;
+    if (PROBE) {
+        probe_out[i] = make_float2(ax + nd, ay + nd);
+        return;
+    }
+    float nx = __fadd_rn(__fadd_rn(p.x, ax), nd);
+    float ny = __fadd_rn(__fadd_rn(p.y, ay), nd);
+    boundary(nx, ny, P, g);
+    const float2 pv = prev[i];
+    const float vx = clamp5(__fdiv_rn(__fsub_rn(nx, pv.x), dt));
+    const float vy = clamp5(__fdiv_rn(__fsub_rn(ny, pv.y), dt));
+    const unsigned k2 = cell_key(nx, ny, g);
+    const unsigned rank = atomicAdd(cnt + k2, 1u);
+    pos_out[i] = make_float2(nx, ny);
+    vel_out[i] = make_float2(vx, vy);
+    kr_out[i] = make_uint2(k2, rank);
+}
+
+// ---------------------------------------------------------------------------
+// state I/O, diagnostics, neighbour lists
+// ---------------------------------------------------------------------------
+
+// Sorted state -> id order: out = [pos | vel | prev | rho | pressure] (5 n float2).
+__global__ void __launch_bounds__(kBlock)
+k_unpermute(int n, const tunable_parameters *__restrict__ dP, const int *__restrict__ id_a,
+            const float2 *__restrict__ pos_a, const float2 *__restrict__ vel_a,
+            const int *__restrict__ id_c, const float2 *__restrict__ prev_c,
+            const float2 *__restrict__ rho_c, float2 *__restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int ia = id_a[i], ic = id_c[i];
+    out[ia] = pos_a[i];
+    out[(size_t)n + ia] = vel_a[i];
+    out[2 * (size_t)n + ic] = prev_c[i];
+    const float2 r = rho_c[i];
+    out[3 * (size_t)n + ic] = r;
+    // pressure and near pressure, fluid.c:563-564
+    out[4 * (size_t)n + ic] = make_float2(__fmul_rn(dP->k, __fsub_rn(r.x, dP->rest_density)),
+                                          __fmul_rn(dP->k_near, r.y));
+}
+
+// Sorted per-particle values -> id order.
+__global__ void __launch_bounds__(kBlock)
+k_by_id(int n, const int *__restrict__ ids, const float2 *__restrict__ in, float2 *__restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[ids[i]] = in[i];
+}
+
+// Uploaded id-order arrays into the *_c slots that download reads before the
+// first step (prev, densities), with the identity id map.
+__global__ void __launch_bounds__(kBlock)
+k_iota(int n, int *__restrict__ ids)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) ids[i] = i;
+}
+
+// Pixel-space shorts for the render rank (fluid.c:360-361), by id.
+__global__ void __launch_bounds__(kBlock)
+k_pack_coords(int n, float max_x, float max_y, const int *__restrict__ id_a,
+              const float2 *__restrict__ pos_a, short2 *__restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float2 p = pos_a[i];
+    const float cx = __fmul_rn(__fsub_rn(__fdiv_rn(__fmul_rn(2.0f, p.x), max_x), 1.0f), 32767.0f);
+    const float cy = __fmul_rn(__fsub_rn(__fdiv_rn(__fmul_rn(2.0f, p.y), max_y), 1.0f), 32767.0f);
+    out[id_a[i]] = make_short2((short)__float2int_rz(cx), (short)__float2int_rz(cy));
+}
+
+// FP64 sums of density, near density and 0.5|v|^2, per block (fixed order).
+__global__ void __launch_bounds__(kBlock)
+k_diag_partial(int n, const float2 *__restrict__ rho_c, const float2 *__restrict__ vel_a,
+               double *__restrict__ partials)
+{
+    __shared__ double sh[3][kBlock / 32];
+    double a = 0.0, b = 0.0, c = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float2 r = rho_c[i];
+        const float2 v = vel_a[i];
+        a += r.x;
+        b += r.y;
+        c += 0.5 * ((double)v.x * v.x + (double)v.y * v.y);
+    }
+    a = warp_sum(a); b = warp_sum(b); c = warp_sum(c);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) { sh[0][warp] = a; sh[1][warp] = b; sh[2][warp] = c; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s0 = 0, s1 = 0, s2 = 0;
+        for (int w = 0; w < kBlock / 32; ++w) { s0 += sh[0][w]; s1 += sh[1][w]; s2 += sh[2][w]; }
+        partials[3 * blockIdx.x] = s0;
+        partials[3 * blockIdx.x + 1] = s1;
+        partials[3 * blockIdx.x + 2] = s2;
+    }
+}
+
+__global__ void k_diag_final(int nparts, int n, const double *__restrict__ partials, double *out)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double s0 = 0, s1 = 0, s2 = 0;
+    for (int b = 0; b < nparts; ++b) {
+        s0 += partials[3 * b];
+        s1 += partials[3 * b + 1];
+        s2 += partials[3 * b + 2];
+    }
+    out[0] = n ? s0 / n : 0.0;
+    out[1] = n ? s1 / n : 0.0;
+    out[2] = n ? s2 / n : 0.0;
+}
+
+// The reference's half list of one particle, in its order (hash.c:169-234):
+// later members of its own cell, then the forward cells (0,+1), (+1,-1),
+// (+1,0), (+1,+1), each in id order, r2 <= h2, cut at max_neighbors.
+// WRITE = false counts, WRITE = true writes ids at out + off[id].
+template <bool WRITE>
+__global__ void __launch_bounds__(kBlock)
+k_half_lists(int n, Grid g, const tunable_parameters *__restrict__ dP,
+             const float2 *__restrict__ pos, const int *__restrict__ ids,
+             const int *__restrict__ start, const unsigned *__restrict__ occ_in,
+             unsigned *__restrict__ counts, const int *__restrict__ off, int *__restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float hh = dP->smoothing_radius;
+    const float h2 = __fmul_rn(hh, hh);
+    const bool capped = *occ_in > (unsigned)g.max_bucket;
+    const float2 p = pos[i];
+    const unsigned key = cell_key(p.x, p.y, g);
+    const int myid = ids[i];
+    int c = 0;
+    int *dst = WRITE ? out + off[myid] : nullptr;
+    if (searchable(key, i, start, g, capped)) {
+        const int gy = (int)(key / (unsigned)g.size_x), gx = (int)key - gy * g.size_x;
+        const int fdx[5] = {0, 0, 1, 1, 1}, fdy[5] = {0, 1, -1, 0, 1};
+        for (int f = 0; f < 5; ++f) {
+            const int x = gx + fdx[f], y = gy + fdy[f];
+            if (x < 0 || y < 0 || x >= g.size_x || y >= g.size_y) continue;
+            const int cell = y * g.size_x + x;
+            const int a = start[cell], e = start[cell + 1];
+            const int b = capped && e - a > g.max_bucket ? a + g.max_bucket : e;
+            for (int j = f == 0 ? i + 1 : a; j < b; ++j) {
+                const float2 q = pos[j];
+                if (dist2(p.x - q.x, p.y - q.y) > h2) continue;
+                if (c < g.max_neighbors) {
+                    if (WRITE) dst[c] = ids[j];
+                    ++c;
+                }
+            }
+        }
+    }
+    if (!WRITE) counts[myid] = (unsigned)c;
+}
+
+// ---------------------------------------------------------------------------
+// host-side launchers
+// ---------------------------------------------------------------------------
+
+static inline int blocks_for(int n) { return (n + kBlock - 1) / kBlock; }
+
+// Exclusive scan of `in` (M entries) into out (M + 1 entries).
+static void launch_scan(sph_cuda *h, unsigned *in, int M, int *out, unsigned *occ, bool zero)
+{
+    const int tiles = (M + kScanTile - 1) / kScanTile;
+    k_scan_reduce<<<tiles, kScanThreads, 0, h->stream>>>(in, M, h->g.ncells, h->tile_sums,
+                                                         h->d_state, occ, h->g.max_bucket,
+                                                         h->g.max_neighbors);
+    k_scan_apply<<<tiles, kScanThreads, 0, h->stream>>>(in, M, h->tile_sums, out, zero ? 1 : 0);
+}
+
+static const char *const kKernelNames[] = {
+    "viscosity_predict", "cell_scan_reduce_1", "cell_scan_apply_1", "cell_scatter_1",
+    "cell_permute_1",    "density",            "relax_update",       "cell_scan_reduce_2",
+    "cell_scan_apply_2", "cell_scatter_2",     "cell_permute_2"};
+static const int kStepKernels = 11;
+
+// Queues one step.  With `events` (kStepKernels + 1 of them) each kernel is
+// bracketed for timing.
+int enqueue_step(sph_cuda *h, cudaEvent_t *events, int *nkernels)
+{
+    const int n = h->n;
+    const int nb = blocks_for(n);
+    const int M = h->g.ncells + 1;
+    const int tiles = (M + kScanTile - 1) / kScanTile;
+    DevState *st = h->d_state;
+    int e = 0;
+    auto mark = [&]() {
+        if (events) cudaEventRecord(events[e], h->stream);
+        ++e;
+    };
+    mark();
+    k_viscosity_predict<false><<<nb, kBlock, 0, h->stream>>>(
+        n, h->g, h->d_params, st, h->pos_a, h->vel_a, h->start_a, &st->build_max_occ[SLOT_RELAXED],
+        &st->build_max_occ[SLOT_PREDICTED], h->pos_b, h->prev_b, h->kr_b, h->cnt, nullptr);
+    mark();
+    k_scan_reduce<<<tiles, kScanThreads, 0, h->stream>>>(h->cnt, M, h->g.ncells, h->tile_sums, st,
+                                                         &st->build_max_occ[SLOT_PREDICTED],
+                                                         h->g.max_bucket, h->g.max_neighbors);
+    mark();
+    k_scan_apply<<<tiles, kScanThreads, 0, h->stream>>>(h->cnt, M, h->tile_sums, h->start_c, 1);
+    mark();
+    k_scatter_ids<<<nb, kBlock, 0, h->stream>>>(n, h->kr_b, h->id_a, h->start_c, h->tmp_id);
+    mark();
+    k_permute<<<nb, kBlock, 0, h->stream>>>(n, h->kr_b, h->start_c, h->tmp_id, h->id_a, h->pos_b,
+                                            h->prev_b, h->id_c, h->pos_c, h->prev_c);
+    mark();
+    k_density<<<nb, kBlock, 0, h->stream>>>(n, h->g, h->d_params, h->pos_c, h->start_c,
+                                            &st->build_max_occ[SLOT_PREDICTED], h->rho_c);
+    mark();
+    k_relax_update<false><<<nb, kBlock, 0, h->stream>>>(
+        n, h->g, h->d_params, h->pos_c, h->rho_c, h->prev_c, h->id_c, h->start_c,
+        &st->build_max_occ[SLOT_PREDICTED], &st->build_max_occ[SLOT_RELAXED], h->pos_b, h->vel_b,
+        h->kr_b, h->cnt, nullptr);
+    mark();
+    k_scan_reduce<<<tiles, kScanThreads, 0, h->stream>>>(h->cnt, M, h->g.ncells, h->tile_sums, st,
+                                                         &st->build_max_occ[SLOT_RELAXED],
+                                                         h->g.max_bucket, h->g.max_neighbors);
+    mark();
+    k_scan_apply<<<tiles, kScanThreads, 0, h->stream>>>(h->cnt, M, h->tile_sums, h->start_a, 1);
+    mark();
+    k_scatter_ids<<<nb, kBlock, 0, h->stream>>>(n, h->kr_b, h->id_c, h->start_a, h->tmp_id);
+    mark();
+    k_permute<<<nb, kBlock, 0, h->stream>>>(n, h->kr_b, h->start_a, h->tmp_id, h->id_c, h->pos_b,
+                                            h->vel_b, h->id_a, h->pos_a, h->vel_a);
+    mark();
+    if (nkernels) *nkernels = e - 1;
+    return cuda_fail(cudaGetLastError(), "step launch");
+}
+
+const char *kernel_name(int k)
+{
+    return (k >= 0 && k < kStepKernels) ? kKernelNames[k] : "";
+}
+int step_kernel_count() { return kStepKernels; }
+
+// Tail of every step (captured in the graph): lists now exist, step counter.
+__global__ void k_end_step(DevState *st)
+{
+    st->lists_valid = 1u;
+    st->steps += 1ull;
+}
+
+void enqueue_end_step(sph_cuda *h)
+{
+    k_end_step<<<1, 1, 0, h->stream>>>(h->d_state);
+}
+
+// Upload tail: pos_b / vel_b (id order) -> sorted A state; prev_c / rho_c
+// already hold the uploaded values in id order.
+int upload_soa_device(sph_cuda *h, int n)
+{
+    const int nb = blocks_for(n);
+    DevState *st = h->d_state;
+    if (n > 0) {
+        k_iota<<<nb, kBlock, 0, h->stream>>>(n, h->id_c);
+        k_keys<<<nb, kBlock, 0, h->stream>>>(n, h->g, h->pos_b, h->kr_b, h->cnt,
+                                             &st->build_max_occ[SLOT_RELAXED]);
+        launch_scan(h, h->cnt, h->g.ncells + 1, h->start_a, &st->build_max_occ[SLOT_RELAXED], true);
+        k_scatter_ids<<<nb, kBlock, 0, h->stream>>>(n, h->kr_b, nullptr, h->start_a, h->tmp_id);
+        k_permute<<<nb, kBlock, 0, h->stream>>>(n, h->kr_b, h->start_a, h->tmp_id, nullptr,
+                                                h->pos_b, h->vel_b, h->id_a, h->pos_a, h->vel_a);
+    }
+    return cuda_fail(cudaGetLastError(), "upload kernels");
+}
+
+int launch_unpermute(sph_cuda *h, float2 *out)
+{
+    if (h->n == 0) return SPH_OK;
+    k_unpermute<<<blocks_for(h->n), kBlock, 0, h->stream>>>(h->n, h->d_params, h->id_a, h->pos_a,
+                                                            h->vel_a, h->id_c, h->prev_c, h->rho_c,
+                                                            out);
+    return cuda_fail(cudaGetLastError(), "unpermute");
+}
+
+int launch_pack(sph_cuda *h, short2 *out)
+{
+    if (h->n == 0) return SPH_OK;
+    k_pack_coords<<<blocks_for(h->n), kBlock, 0, h->stream>>>(h->n, h->g.max_x, h->g.max_y,
+                                                              h->id_a, h->pos_a, out);
+    return cuda_fail(cudaGetLastError(), "pack coords");
+}
+
+int launch_diagnostics(sph_cuda *h, double *d_out)
+{
+    const int parts = h->npartials;
+    k_diag_partial<<<parts, kBlock, 0, h->stream>>>(h->n, h->rho_c, h->vel_a, h->d_partials);
+    k_diag_final<<<1, 32, 0, h->stream>>>(parts, h->n, h->d_partials, d_out);
+    return cuda_fail(cudaGetLastError(), "diagnostics");
+}
+
+// Probes on the A state.  which: 0 density, 1 relaxation displacement,
+// 2 viscosity velocity change.  out: n float2 by id (device).
+int launch_probe(sph_cuda *h, int which, float2 *tmp_sorted, float2 *tmp_rho, float2 *out)
+{
+    const int n = h->n;
+    if (n == 0) return SPH_OK;
+    const int nb = blocks_for(n);
+    DevState *st = h->d_state;
+    const unsigned *occ = &st->build_max_occ[SLOT_RELAXED];
+    if (which == 0 || which == 1) {
+        k_density<<<nb, kBlock, 0, h->stream>>>(n, h->g, h->d_params, h->pos_a, h->start_a, occ,
+                                                which == 0 ? tmp_sorted : tmp_rho);
+        if (which == 1)
+            k_relax_update<true><<<nb, kBlock, 0, h->stream>>>(
+                n, h->g, h->d_params, h->pos_a, tmp_rho, nullptr, h->id_a, h->start_a, occ,
+                nullptr, nullptr, nullptr, nullptr, nullptr, tmp_sorted);
+    } else {
+        k_viscosity_predict<true><<<nb, kBlock, 0, h->stream>>>(
+            n, h->g, h->d_params, st, h->pos_a, h->vel_a, h->start_a, occ, nullptr, nullptr,
+            nullptr, nullptr, nullptr, tmp_sorted);
+    }
+    k_by_id<<<nb, kBlock, 0, h->stream>>>(n, h->id_a, tmp_sorted, out);
+    return cuda_fail(cudaGetLastError(), "probe");
+}
+
+// Half lists in the reference's order on the A state.  d_counts: n + 1
+// words (scanned in place into offsets), d_off: n + 1 ints.
+int launch_half_lists(sph_cuda *h, unsigned *d_counts, int *d_off, int *d_ids, bool write)
+{
+    const int n = h->n;
+    if (n == 0) return SPH_OK;
+    const int nb = blocks_for(n);
+    const unsigned *occ = &h->d_state->build_max_occ[SLOT_RELAXED];
+    if (!write) {
+        k_half_lists<false><<<nb, kBlock, 0, h->stream>>>(n, h->g, h->d_params, h->pos_a, h->id_a,
+                                                          h->start_a, occ, d_counts, nullptr,
+                                                          nullptr);
+        launch_scan(h, d_counts, n, d_off, nullptr, false);
+    } else {
+        k_half_lists<true><<<nb, kBlock, 0, h->stream>>>(n, h->g, h->d_params, h->pos_a, h->id_a,
+                                                         h->start_a, occ, nullptr, d_off, d_ids);
+    }
+    return cuda_fail(cudaGetLastError(), "half lists");
+}
+
+}  // namespace sph

@@ -1,0 +1,188 @@
+"""Synthetic scenes for the SPH compute step (dam breaks and ensembles).
+
+Every scene is reproducible from its seed with a documented generator
+(splitmix64 counters -> uniform doubles), so the CUDA library and the CPU
+oracle receive bit-identical float32 inputs.
+
+Dam break (the reference's lattice fill, geometry.c:29-67, moved into a box
+corner): particles on a square lattice of spacing 0.5h filling a block from
+the box floor at the left wall, row-major from (0, 0), `cols` particles per
+row, jittered by U(-0.01h, 0.01h) per axis, zero velocity.  Smoothing radius
+h = 1, neighbour-grid spacing h (fluid.c:176), grid size ceil(box/h)
+(fluid.c:214-215), bucket cap 100 and list cap 400 (fluid.c:174-175).
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+SPHERE_MOVER = 0      # fluid.h:48
+RECTANGLE_MOVER = 1   # fluid.h:49
+
+_M64 = np.uint64(0xFFFFFFFFFFFFFFFF)
+
+
+def splitmix64(seed: int, counters: np.ndarray) -> np.ndarray:
+    """splitmix64 output for each counter value (uint64 array)."""
+    with np.errstate(over="ignore"):
+        z = np.uint64(seed) + (counters.astype(np.uint64) + np.uint64(1)) * np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    return z
+
+
+def uniform(seed: int, counters: np.ndarray) -> np.ndarray:
+    """Uniform doubles in [0, 1): top 53 bits of splitmix64."""
+    return (splitmix64(seed, counters) >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+
+
+@dataclass
+class Params:
+    """The reference's tunable_parameters (fluid.h:78-97), by field name."""
+    rest_density: float = 1.3
+    smoothing_radius: float = 1.0
+    g: float = 9.8               # apply_gravity applies -g (fluid.c:403)
+    k: float = 0.3
+    k_near: float = 1.5
+    k_spring: float = 10.0       # reference default, fluid.c:94
+    sigma: float = 0.5
+    beta: float = 0.1
+    time_step: float = 1.0 / 60.0
+    node_start_x: float = 0.0
+    node_end_x: float = 0.0
+    mover_center_x: float = -1000.0
+    mover_center_y: float = -1000.0
+    mover_width: float = 0.0
+    mover_height: float = 0.0
+    mover_type: int = SPHERE_MOVER
+    kill_sim: int = 0
+    active: int = 1
+
+    FIELDS = ("rest_density", "smoothing_radius", "g", "k", "k_near", "k_spring", "sigma",
+              "beta", "time_step", "node_start_x", "node_end_x", "mover_center_x",
+              "mover_center_y", "mover_width", "mover_height")
+
+    def as_dict(self) -> dict:
+        d = {f: float(getattr(self, f)) for f in self.FIELDS}
+        d.update(mover_type=int(self.mover_type), kill_sim=int(self.kill_sim), active=int(self.active))
+        return d
+
+
+@dataclass
+class Scene:
+    name: str
+    x: np.ndarray          # float32 [n]
+    y: np.ndarray
+    vx: np.ndarray
+    vy: np.ndarray
+    box: tuple             # (min_x, max_x, min_y, max_y)
+    params: Params
+    spacing: float = 1.0
+    size_x: int = 0
+    size_y: int = 0
+    max_bucket: int = 100
+    max_neighbors: int = 400
+    steps: int = 1000
+    mover_period: float = 0.0     # steps; 0 = static mover
+    mover_amplitude: float = 0.0
+    mover_base: tuple = (0.0, 0.0)
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def n(self) -> int:
+        return int(self.x.shape[0])
+
+    @property
+    def cells(self) -> int:
+        return self.size_x * self.size_y
+
+    def mover_at(self, t: int) -> tuple:
+        """Mover centre set before step t (float32 values)."""
+        if self.mover_period <= 0.0:
+            return (np.float32(self.params.mover_center_x), np.float32(self.params.mover_center_y))
+        cx = self.mover_base[0] + self.mover_amplitude * math.sin(2.0 * math.pi * t / self.mover_period)
+        return (np.float32(cx), np.float32(self.mover_base[1]))
+
+    def mover_schedule(self, t0: int, nsteps: int) -> np.ndarray:
+        """[nsteps, 2] float32 mover centres for steps t0 .. t0+nsteps-1."""
+        out = np.empty((nsteps, 2), np.float32)
+        for i in range(nsteps):
+            out[i] = self.mover_at(t0 + i)
+        return out
+
+    def params_at(self, t: int) -> Params:
+        p = Params(**{k: getattr(self.params, k) for k in Params.FIELDS},
+                   mover_type=self.params.mover_type, kill_sim=0, active=1)
+        p.mover_center_x, p.mover_center_y = (float(v) for v in self.mover_at(t))
+        return p
+
+    def config(self) -> dict:
+        return dict(box=tuple(float(b) for b in self.box), spacing=float(self.spacing),
+                    size_x=self.size_x, size_y=self.size_y, max_bucket=self.max_bucket,
+                    max_neighbors=self.max_neighbors)
+
+
+def dam_break(n: int, cols: int, box_w: float, box_h: float, seed: int, *, name: str,
+              params: Params | None = None, lattice: float = 0.5, jitter: float = 0.01,
+              x0: float = 0.0, y0: float = 0.0) -> Scene:
+    """Lattice block of `n` particles, `cols` per row, from (x0, y0)."""
+    i = np.arange(n, dtype=np.int64)
+    row, col = np.divmod(i, cols)
+    u = uniform(seed, np.arange(2 * n, dtype=np.uint64)).reshape(n, 2)
+    jx = (u[:, 0] * 2.0 - 1.0) * jitter
+    jy = (u[:, 1] * 2.0 - 1.0) * jitter
+    x = (x0 + col * lattice + jx).astype(np.float32)
+    y = (y0 + row * lattice + jy).astype(np.float32)
+    p = params or Params()
+    p.node_start_x = 0.0
+    p.node_end_x = float(box_w)
+    h = float(p.smoothing_radius)
+    sc = Scene(name=name, x=x, y=y, vx=np.zeros(n, np.float32), vy=np.zeros(n, np.float32),
+               box=(0.0, float(box_w), 0.0, float(box_h)), params=p, spacing=h,
+               size_x=int(math.ceil(box_w / h)), size_y=int(math.ceil(box_h / h)))
+    return sc
+
+
+def config1() -> Scene:
+    """3,000-particle dam break in a 96h x 48h box (64 particles per row, 46
+    full rows + 56), no mover, 1,000 steps, seed 1001."""
+    s = dam_break(3000, 64, 96.0, 48.0, seed=1001, name="dam_break_3k_96x48")
+    s.steps = 1000
+    return s
+
+
+def config2(n: int = 4_194_304) -> Scene:
+    """4,194,304-particle dam break: box 3,590h x 1,795h keeps config 1's fill
+    fraction (0.1627) and 2:1 aspect; 2,393 particles per row (x <= 1,196h),
+    1,752 full rows + 1,768; sphere mover of width 16h (radius 8h, fluid.c:666)
+    centred at (598 + 20 sin(2 pi t / 240), 438), 1,000 steps, seed 1002.
+
+    Smaller `n` gives the same construction scaled by sqrt(n / 4,194,304)
+    (box, columns, mover centre and amplitude; radius kept at 8h)."""
+    if n == 4_194_304:
+        box_w, box_h, cols = 3590.0, 1795.0, 2393
+        base, amp = (598.0, 438.0), 20.0
+    else:
+        s = math.sqrt(n / 4_194_304)
+        box_w, box_h = float(math.ceil(3590 * s)), float(math.ceil(1795 * s))
+        cols = max(8, int(round(2393 * s)))
+        base, amp = (round(598 * s, 3), round(438 * s, 3)), max(1.0, round(20 * s, 3))
+    p = Params(mover_type=SPHERE_MOVER, mover_width=16.0, mover_height=16.0)
+    sc = dam_break(n, cols, box_w, box_h, seed=1002, name=f"dam_break_{n}", params=p)
+    sc.steps = 1000
+    sc.mover_period = 240.0
+    sc.mover_amplitude = amp
+    sc.mover_base = base
+    sc.params.mover_center_x, sc.params.mover_center_y = (float(v) for v in sc.mover_at(0))
+    return sc
+
+
+def algorithmic_bytes_per_step(n: int, cells: int) -> int:
+    """Canonical algorithmic HBM bytes of one step: 216 B per particle
+    (viscosity+predict 40, cell build on predicted positions 68, density 16,
+    relaxation+update 40, cell build on relaxed positions 52) + 16 B per
+    cell (cell start/count written and read by both builds)."""
+    return 216 * n + 16 * cells

@@ -1,0 +1,212 @@
+"""Python host wrapper of the libsph_cuda fast API (include/sph_cuda.h).
+
+`Simulation` owns one library handle: one single-device SPH domain whose
+particle state stays in GPU memory between steps.  Every method maps to one
+C-ABI call; arrays cross the boundary as host numpy buffers.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import (AABB, Counters, NeighborGrid, Param, PARTICLE_DTYPE, check, lib,
+                   tunables)
+
+
+def _f(a):
+    return a.ctypes.data_as(_lib.c_float_p)
+
+
+class Simulation:
+    """One compute rank's domain on the GPU.
+
+    params : dict of tunable_parameters fields (smoothing_radius = h)
+    config : dict(box=(min_x, max_x, min_y, max_y), spacing, size_x, size_y,
+             max_bucket, max_neighbors) -- the reference's grid set-up
+             (fluid.c:173-176, 214-215)
+    capacity : maximum particle count of the handle
+    """
+
+    def __init__(self, params: dict, config: dict, capacity: int):
+        self._h = ctypes.c_void_p()
+        p = Param()
+        p.tunable_params = tunables(params)
+        p.number_fluid_particles_global = capacity
+        p.number_fluid_particles_local = capacity
+        p.max_fluid_particle_index = capacity - 1
+        p.number_halo_particles = 0
+        b = AABB()
+        b.min_x, b.max_x, b.min_y, b.max_y = (float(v) for v in config["box"])
+        g = NeighborGrid()
+        g.spacing = config["spacing"]
+        g.size_x, g.size_y = config["size_x"], config["size_y"]
+        g.max_bucket_size = config["max_bucket"]
+        g.max_neighbors = config["max_neighbors"]
+        check(lib().sph_cuda_create(ctypes.byref(self._h), ctypes.byref(p), ctypes.byref(b),
+                                    ctypes.byref(g), int(capacity)))
+        self.params = dict(params)
+        self.config = dict(config)
+        self.capacity = int(capacity)
+        self.n = 0
+
+    @classmethod
+    def from_scene(cls, scene, capacity: int | None = None) -> "Simulation":
+        sim = cls(scene.params.as_dict(), scene.config(), capacity or scene.n)
+        sim.upload(scene.x, scene.y, scene.vx, scene.vy)
+        return sim
+
+    # -- lifecycle ---------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            lib().sph_cuda_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._h
+
+    # -- state -------------------------------------------------------------
+    def upload(self, x, y, vx=None, vy=None):
+        arrs = [None if a is None else np.ascontiguousarray(a, np.float32) for a in (x, y, vx, vy)]
+        n = len(arrs[0])
+        check(lib().sph_cuda_upload_soa(self._h, *[None if a is None else _f(a) for a in arrs], n))
+        self.n = n
+
+    def upload_particles(self, particles: np.ndarray):
+        """particles: structured array of PARTICLE_DTYPE (fluid_particle)."""
+        a = np.ascontiguousarray(particles, PARTICLE_DTYPE)
+        check(lib().sph_cuda_upload_particles(self._h, a.ctypes.data, len(a)))
+        self.n = len(a)
+
+    def download(self) -> dict:
+        n = self.n
+        out = {k: np.empty(n, np.float32) for k in ("x", "y", "v_x", "v_y", "density", "density_near")}
+        check(lib().sph_cuda_download_soa(self._h, _f(out["x"]), _f(out["y"]), _f(out["v_x"]),
+                                          _f(out["v_y"]), _f(out["density"]),
+                                          _f(out["density_near"]), n))
+        return out
+
+    def download_particles(self) -> np.ndarray:
+        a = np.zeros(self.n, PARTICLE_DTYPE)
+        a["id"] = np.arange(self.n)
+        check(lib().sph_cuda_download_particles(self._h, a.ctypes.data, self.n))
+        return a
+
+    def pack_coords(self, out: np.ndarray | None = None) -> np.ndarray:
+        if out is None:
+            out = np.empty((self.n, 2), np.int16)
+        check(lib().sph_cuda_pack_coords_short(self._h, out.ctypes.data_as(_lib.c_short_p), self.n))
+        return out
+
+    # -- stepping ------------------------------------------------------------
+    def step(self, params: dict | None = None, nsteps: int = 1):
+        t = tunables(params or self.params)
+        check(lib().sph_cuda_step(self._h, ctypes.byref(t), int(nsteps)))
+
+    def step_schedule(self, params_list: list):
+        arr = (_lib.TunableParameters * len(params_list))(*[tunables(p) for p in params_list])
+        check(lib().sph_cuda_step_schedule(self._h, arr, len(params_list)))
+
+    def rebuild_neighbors(self):
+        check(lib().sph_cuda_rebuild_neighbors(self._h))
+
+    def synchronize(self):
+        check(lib().sph_cuda_synchronize(self._h))
+
+    # -- inspection ------------------------------------------------------------
+    def diagnostics(self) -> np.ndarray:
+        out = np.zeros(3, np.float64)
+        check(lib().sph_cuda_diagnostics(self._h, out.ctypes.data_as(_lib.c_double_p)))
+        return out
+
+    def counters(self) -> dict:
+        c = Counters()
+        check(lib().sph_cuda_get_counters(self._h, ctypes.byref(c)))
+        return {k: getattr(c, k) for k, _ in Counters._fields_}
+
+    def neighbor_lists(self):
+        counts = np.zeros(max(self.n, 1), np.int32)
+        total = ctypes.c_longlong(0)
+        st = lib().sph_cuda_neighbor_lists(self._h, counts.ctypes.data_as(_lib.c_int_p), None, 0,
+                                           ctypes.byref(total))
+        if st not in (0, 4):
+            check(st)
+        ids = np.zeros(max(total.value, 1), np.int32)
+        check(lib().sph_cuda_neighbor_lists(self._h, counts.ctypes.data_as(_lib.c_int_p),
+                                            ids.ctypes.data_as(_lib.c_int_p), total.value,
+                                            ctypes.byref(total)))
+        return counts[:self.n].copy(), ids[:total.value].copy()
+
+    def _probe(self, fn, params):
+        t = tunables(params or self.params)
+        a = np.zeros(self.n, np.float32)
+        b = np.zeros(self.n, np.float32)
+        check(fn(self._h, ctypes.byref(t), _f(a), _f(b)))
+        return a, b
+
+    def probe_density(self, params: dict | None = None):
+        return self._probe(lib().sph_cuda_probe_density, params)
+
+    def probe_relaxation(self, params: dict | None = None):
+        return self._probe(lib().sph_cuda_probe_relaxation, params)
+
+    def probe_viscosity(self, params: dict | None = None):
+        return self._probe(lib().sph_cuda_probe_viscosity, params)
+
+    def kernel_times(self, params: dict | None = None) -> dict:
+        """Runs ONE step with per-kernel CUDA events; {kernel name: ms}."""
+        t = tunables(params or self.params)
+        ms = np.zeros(32, np.float32)
+        cnt = ctypes.c_int(0)
+        check(lib().sph_cuda_kernel_times(self._h, ctypes.byref(t), _f(ms), 32, ctypes.byref(cnt)))
+        return {lib().sph_cuda_kernel_name(k).decode(): float(ms[k]) for k in range(cnt.value)}
+
+    def launches_per_step(self) -> int:
+        return int(lib().sph_cuda_launches_per_step(self._h))
+
+    def timer_start(self):
+        check(lib().sph_cuda_timer_start(self._h))
+
+    def timer_stop(self) -> float:
+        """Milliseconds on the handle's stream since timer_start (synchronises)."""
+        ms = ctypes.c_float(0.0)
+        check(lib().sph_cuda_timer_stop(self._h, ctypes.byref(ms)))
+        return float(ms.value)
+
+
+class PinnedArray:
+    """numpy view of page-locked host memory from sph_cuda_host_alloc."""
+
+    def __init__(self, shape, dtype):
+        self.dtype = np.dtype(dtype)
+        nbytes = int(np.prod(shape)) * self.dtype.itemsize
+        self._p = ctypes.c_void_p()
+        check(lib().sph_cuda_host_alloc(ctypes.byref(self._p), nbytes))
+        buf = (ctypes.c_byte * max(nbytes, 1)).from_address(self._p.value)
+        self.array = np.frombuffer(buf, self.dtype, count=int(np.prod(shape))).reshape(shape)
+
+    def free(self):
+        if self._p.value:
+            self.array = None
+            lib().sph_cuda_host_free(self._p)
+            self._p = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass

@@ -1,0 +1,315 @@
+"""Parity of the CUDA step against the reference, layer by layer.
+
+1. neighbour lists: bit-exact against the reference's hash_fluid output on
+   identical positions (golden vectors from the compiled reference);
+2. density / near density: within 1e-5 relative of the reference's own
+   hash_fluid(.., true) densities;
+3. relaxation displacement and viscosity velocity change: within 1e-5 of
+   the FP64 gather oracle, relative to the summed magnitude of the terms;
+4. 1,000-step runs: mean density and kinetic energy within 2% of the
+   reference's Gauss-Seidel loop;
+plus edge cases (caps, aliasing, empty input, non-finite input), the render
+packing, upload/download, determinism.  Every call goes through the C ABI.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import EDGE_CONFIG, bits_equal, golden
+from sph_gb300 import PARTICLE_DTYPE, Simulation, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def sim_for(x, y, vx=None, vy=None, params=None, config=None, capacity=None):
+    params = params or scenes.Params().as_dict()
+    s = Simulation(params, config, capacity or max(len(x), 1))
+    s.upload(x, y, vx, vy)
+    return s
+
+
+def cfg1():
+    sc = scenes.config1()
+    return sc, sc.params.as_dict(), sc.config()
+
+
+# ---------------------------------------------------------------- layer 1
+@pytest.mark.parametrize("t", [100, 1000])
+def test_neighbor_lists_bit_exact(cuda_lib, t):
+    g = golden("cfg1")
+    sc, P, C = cfg1()
+    with sim_for(g[f"s{t}_x"], g[f"s{t}_y"], params=P, config=C) as s:
+        counts, ids = s.neighbor_lists()
+    assert np.array_equal(counts, g[f"h{t}_counts"])
+    assert np.array_equal(ids, g[f"h{t}_ids"])
+
+
+@pytest.mark.parametrize("name,pre", [("edges", "edge"), ("listcap", "cap")])
+def test_neighbor_lists_edge_cases(cuda_lib, name, pre):
+    g = golden(name)
+    with sim_for(g["x"], g["y"], config=EDGE_CONFIG) as s:
+        counts, ids = s.neighbor_lists()
+        c = s.counters()
+    assert np.array_equal(counts, g[f"{pre}_counts"])
+    assert np.array_equal(ids, g[f"{pre}_ids"])
+    if name == "edges":
+        assert c["bucket_overflow"] == 30 and c["max_cell_occupancy"] == 130
+    else:
+        assert c["list_cap_risk"] == 1
+
+
+def test_mover_scene_lists(cuda_lib):
+    g = golden("mover")
+    sc = scenes.config2(n=4096)
+    for tag in ("sphere", "rect"):
+        with sim_for(g[f"{tag}_s100_x"], g[f"{tag}_s100_y"], config=sc.config()) as s:
+            counts, ids = s.neighbor_lists()
+        assert np.array_equal(counts, g[f"{tag}_h100_counts"])
+        assert np.array_equal(ids, g[f"{tag}_h100_ids"])
+
+
+# ---------------------------------------------------------------- layer 2
+def _rel_ok(a, b, rtol=1e-5, atol=1e-7):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return np.all(np.abs(a - b) <= rtol * np.abs(b) + atol), float(
+        np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-30) * (np.abs(b) > 1e-3), initial=0))
+
+
+@pytest.mark.parametrize("t", [100, 1000])
+def test_density_matches_reference(cuda_lib, t):
+    g = golden("cfg1")
+    sc, P, C = cfg1()
+    with sim_for(g[f"s{t}_x"], g[f"s{t}_y"], params=P, config=C) as s:
+        rho, rhon = s.probe_density(P)
+    ok, err = _rel_ok(rho, g[f"h{t}_rho"])
+    assert ok, err
+    ok, err = _rel_ok(rhon, g[f"h{t}_rhon"])
+    assert ok, err
+
+
+def test_density_edge_cases(cuda_lib):
+    g = golden("edges")
+    with sim_for(g["x"], g["y"], config=EDGE_CONFIG) as s:
+        rho, rhon = s.probe_density()
+    ok, err = _rel_ok(rho, g["edge_rho"])
+    assert ok, err
+    ok, err = _rel_ok(rhon, g["edge_rhon"])
+    assert ok, err
+    assert (rho[100:130] == 0).all()  # beyond the bucket cap: never inserted
+
+
+# ---------------------------------------------------------------- layer 3
+def _fp64_check(got, want, scale, tol=1e-5):
+    err = np.abs(np.asarray(got, np.float64) - want)
+    bound = tol * scale + 1e-9
+    return np.all(err <= bound), float(np.max(err / (scale + 1e-30)))
+
+
+@pytest.mark.parametrize("t", [1, 100, 1000])
+def test_relaxation_displacement_fp64(cuda_lib, t):
+    g = golden("cfg1")
+    sc, P, C = cfg1()
+    x, y = g[f"s{t}_x"], g[f"s{t}_y"]
+    with sim_for(x, y, params=P, config=C) as s:
+        rho, rhon = s.probe_density(P)
+        dx, dy = s.probe_relaxation(P)
+    z = np.zeros_like(x)
+    orc = oracle.Sim("port", x, y, z, z, P, C)
+    orc.hash(compute_density=False)
+    ox, oy, scale = orc.relax_f64(rho, rhon)
+    assert np.abs(ox).max() > 1e-4  # a real displacement field
+    for got, want in ((dx, ox), (dy, oy)):
+        ok, err = _fp64_check(got, want, scale)
+        assert ok, err
+    # and against the FP64 densities as inputs (end-to-end density + relaxation)
+    r64, rn64 = orc.density_f64()
+    ox2, oy2, scale2 = orc.relax_f64(r64.astype(np.float32), rn64.astype(np.float32))
+    for got, want in ((dx, ox2), (dy, oy2)):
+        ok, err = _fp64_check(got, want, scale2)
+        assert ok, err
+
+
+@pytest.mark.parametrize("t", [10, 100, 1000])
+def test_viscosity_fp64(cuda_lib, t):
+    g = golden("cfg1")
+    sc, P, C = cfg1()
+    x, y, vx, vy = (g[f"s{t}_{k}"] for k in ("x", "y", "v_x", "v_y"))
+    with sim_for(x, y, vx, vy, params=P, config=C) as s:
+        dvx, dvy = s.probe_viscosity(P)
+    orc = oracle.Sim("port", x, y, vx, vy, P, C)
+    orc.hash(compute_density=False)
+    ox, oy, scale = orc.viscosity_f64()
+    assert np.abs(ox).max() > 1e-5
+    for got, want in ((dvx, ox), (dvy, oy)):
+        ok, err = _fp64_check(got, want, scale)
+        assert ok, err
+
+
+# ---------------------------------------------------------------- layer 4
+def test_drift_1000_steps_within_2_percent(cuda_lib):
+    g = golden("cfg1")["diag"]
+    sc, P, C = cfg1()
+    d = np.zeros((1000, 3))
+    with Simulation.from_scene(sc) as s:
+        for t in range(1000):
+            s.step(P)
+            d[t] = s.diagnostics()
+    for col in (0, 2):  # mean density, kinetic energy
+        assert abs(d[-1, col] - g[-1, col]) / g[-1, col] < 0.02, (col, d[-1], g[-1])
+        assert abs(d[:, col].mean() - g[:, col].mean()) / g[:, col].mean() < 0.02
+
+
+def test_first_steps_match_cpu_jacobi(cuda_lib):
+    sc, P, C = cfg1()
+    orc = oracle.Sim("port", sc.x, sc.y, sc.vx, sc.vy, P, C)
+    with Simulation.from_scene(sc) as s:
+        done = 0
+        for t, atol in ((1, 2e-5), (10, 2e-4)):
+            s.step(P, t - done)
+            orc.step(t - done, jacobi=True)
+            done = t
+            a, b = s.download(), orc.get()
+            for k in ("x", "y"):
+                assert np.abs(a[k] - b[k]).max() < atol, (t, k, np.abs(a[k] - b[k]).max())
+            for k in ("v_x", "v_y"):
+                assert np.abs(a[k] - b[k]).max() < atol * 60, (t, k)
+
+
+@pytest.mark.parametrize("tag", ["sphere", "rect"])
+def test_mover_steps_match_cpu_jacobi(cuda_lib, tag):
+    sc = scenes.config2(n=4096)
+    sc.params.mover_type = scenes.SPHERE_MOVER if tag == "sphere" else scenes.RECTANGLE_MOVER
+    sc.params.mover_width, sc.params.mover_height = (16.0, 16.0) if tag == "sphere" else (12.0, 6.0)
+    P, C = sc.params.as_dict(), sc.config()
+    mv = sc.mover_schedule(0, 20)
+    orc = oracle.Sim("port", sc.x, sc.y, sc.vx, sc.vy, P, C)
+    od = orc.step(20, mv, jacobi=True)
+    with Simulation.from_scene(sc) as s:
+        s.step_schedule([sc.params_at(t).as_dict() for t in range(20)])
+        a = s.download()
+        gd = s.diagnostics()
+    b = orc.get()
+    assert np.abs(a["x"] - b["x"]).max() < 1e-3 and np.abs(a["y"] - b["y"]).max() < 1e-3
+    assert np.allclose(gd, od[-1], rtol=1e-3)
+
+
+def test_rebuild_neighbors_enables_first_step_viscosity(cuda_lib):
+    g = golden("cfg1")
+    sc, P, C = cfg1()
+    x, y, vx, vy = (g[f"s100_{k}"] for k in ("x", "y", "v_x", "v_y"))
+    orc = oracle.Sim("port", x, y, vx, vy, P, C)
+    orc.hash(compute_density=False)
+    orc.step(1, jacobi=True)
+    with sim_for(x, y, vx, vy, params=P, config=C) as s:
+        s.rebuild_neighbors()
+        s.step(P)
+        a = s.download()
+    b = orc.get()
+    assert np.abs(a["v_x"] - b["v_x"]).max() < 1e-3
+    assert np.abs(a["x"] - b["x"]).max() < 2e-5
+
+
+# ---------------------------------------------------------------- I/O, edges
+def test_pack_coords_exact(cuda_lib):
+    sc, P, C = cfg1()
+    with Simulation.from_scene(sc) as s:
+        s.step(P, 50)
+        st = s.download()
+        coords = s.pack_coords()
+    orc = oracle.Sim("port", st["x"], st["y"], st["v_x"], st["v_y"], P, C)
+    assert np.array_equal(coords, orc.pack_coords())
+
+
+def test_upload_download_particles_roundtrip(cuda_lib):
+    sc, P, C = cfg1()
+    rng = np.random.default_rng(5)
+    a = np.zeros(sc.n, PARTICLE_DTYPE)
+    a["x"], a["y"] = sc.x, sc.y
+    for f in ("x_prev", "y_prev", "v_x", "v_y", "density", "density_near"):
+        a[f] = rng.random(sc.n).astype(np.float32)
+    a["id"] = np.arange(sc.n)
+    with Simulation(P, C, sc.n) as s:
+        s.upload_particles(a)
+        b = s.download_particles()
+    for f in ("x", "y", "x_prev", "y_prev", "v_x", "v_y", "density", "density_near"):
+        assert bits_equal(a[f], b[f]), f
+    assert np.allclose(b["pressure"], np.float32(P["k"]) * (a["density"] - np.float32(P["rest_density"])))
+
+
+def test_upload_through_pointer_array(cuda_lib):
+    from sph_gb300 import _lib
+    sc, P, C = cfg1()
+    n = 257
+    parts = (_lib.FluidParticle * n)()
+    for i in range(n):
+        parts[i].x, parts[i].y, parts[i].v_x, parts[i].id = float(sc.x[i]), float(sc.y[i]), 0.5, i
+    ptrs = (ctypes.POINTER(_lib.FluidParticle) * n)(*[ctypes.pointer(parts[n - 1 - i]) for i in range(n)])
+    with Simulation(P, C, n) as s:
+        _lib.check(_lib.lib().sph_cuda_upload(s.handle, ptrs, n))
+        s.n = n
+        s.step(P, 3)
+        _lib.check(_lib.lib().sph_cuda_download(s.handle, ptrs, n))
+        st = s.download()
+    # pointer i refers to parts[n-1-i]: the state written back must follow the pointers
+    got_x = np.array([parts[n - 1 - i].x for i in range(n)], np.float32)
+    assert bits_equal(got_x, st["x"])
+
+
+def test_empty_scene(cuda_lib):
+    sc, P, C = cfg1()
+    with Simulation(P, C, 16) as s:
+        s.upload(np.zeros(0, np.float32), np.zeros(0, np.float32))
+        s.step(P, 5)
+        assert s.download()["x"].shape == (0,)
+        assert np.array_equal(s.diagnostics(), np.zeros(3))
+        counts, ids = s.neighbor_lists()
+        assert counts.shape == (0,) and ids.shape == (0,)
+
+
+def test_capacity_and_argument_errors(cuda_lib):
+    from sph_gb300 import SphError
+    sc, P, C = cfg1()
+    with Simulation(P, C, 10) as s:
+        with pytest.raises(SphError) as e:
+            s.upload(sc.x[:11], sc.y[:11])
+        assert e.value.status == 4
+        bad = dict(P, time_step=0.0)
+        s.upload(sc.x[:10], sc.y[:10])
+        with pytest.raises(SphError):
+            s.step(bad)
+
+
+def test_nonfinite_particle_is_isolated(cuda_lib):
+    sc, P, C = cfg1()
+    x = sc.x.copy()
+    x[7] = np.nan
+    with sim_for(x, sc.y, params=P, config=C) as s:
+        s.step(P, 10)
+        st = s.download()
+        c = s.counters()
+    others = np.isfinite(st["x"])
+    assert others.sum() == sc.n - 1 and not others[7]
+    assert c["out_of_grid"] >= 20 and c["steps"] == 10
+
+
+def test_deterministic(cuda_lib):
+    sc = scenes.config2(n=4096)
+    outs = []
+    for _ in range(2):
+        with Simulation.from_scene(sc) as s:
+            s.step_schedule([sc.params_at(t).as_dict() for t in range(30)])
+            outs.append(s.download())
+    for k in outs[0]:
+        assert bits_equal(outs[0][k], outs[1][k]), k
+
+
+def test_kernel_times(cuda_lib):
+    sc, P, C = cfg1()
+    with Simulation.from_scene(sc) as s:
+        s.step(P, 3)
+        times = s.kernel_times(P)
+        assert s.launches_per_step() == 12
+    assert len(times) == 11 and all(v > 0 for v in times.values())
