@@ -13,9 +13,9 @@ namespace sph {
 int launch_unpermute(sph_cuda *h, float2 *out);
 int launch_pack(sph_cuda *h, short2 *out);
 int launch_diagnostics(sph_cuda *h, double *d_out);
-int launch_probe(sph_cuda *h, int which, float2 *tmp_sorted, float2 *tmp_rho, float2 *out);
+int launch_probe(sph_cuda *h, int which, void *scratch, float2 *out);
+size_t probe_scratch_bytes(int n);
 int launch_half_lists(sph_cuda *h, unsigned *d_counts, int *d_off, int *d_ids, bool write);
-void enqueue_end_step(sph_cuda *h);
 const char *kernel_name(int k);
 int step_kernel_count();
 
@@ -89,7 +89,6 @@ static int capture_step(sph_cuda *h)
     SPH_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     int nk = 0;
     int rc = enqueue_step(h, nullptr, &nk);
-    enqueue_end_step(h);
     cudaGraph_t g = nullptr;
     const cudaError_t ce = cudaStreamEndCapture(h->stream, &g);
     if (rc != SPH_OK) {
@@ -100,7 +99,7 @@ static int capture_step(sph_cuda *h)
     h->graph = g;
     SPH_CUDA(cudaGraphInstantiate(&h->exec, g, 0));
     h->graph_n = h->n;
-    h->launches_per_step = nk + 1;
+    h->launches_per_step = nk;
     return SPH_OK;
 }
 
@@ -169,15 +168,16 @@ static int upload_common(sph_cuda *h, int n, Fill fill)
 {
     SPH_TRY(check_n(h, n));
     SPH_CUDA(cudaStreamSynchronize(h->stream));
-    SPH_TRY(ensure_stage(h, (size_t)n * 4 * sizeof(float2) + 16));
-    float2 *pos = (float2 *)h->h_stage, *vel = pos + n, *prev = vel + n, *rho = prev + n;
+    SPH_TRY(ensure_stage(h, (size_t)n * 5 * sizeof(float2) + 16));
+    float4 *xr = (float4 *)h->h_stage;
+    float2 *pos = (float2 *)(xr + n), *vel = pos + n, *prev = vel + n;
     for (int i = 0; i < n; ++i) {
         float r[8];
         fill(i, r);
         pos[i] = make_float2(r[0], r[1]);
         vel[i] = make_float2(r[2], r[3]);
         prev[i] = make_float2(r[4], r[5]);
-        rho[i] = make_float2(r[6], r[7]);
+        xr[i] = make_float4(r[0], r[1], r[6], r[7]);
     }
     h->n = n;
     const size_t b = (size_t)n * sizeof(float2);
@@ -185,7 +185,7 @@ static int upload_common(sph_cuda *h, int n, Fill fill)
         SPH_CUDA(cudaMemcpyAsync(h->pos_b, pos, b, cudaMemcpyHostToDevice, h->stream));
         SPH_CUDA(cudaMemcpyAsync(h->vel_b, vel, b, cudaMemcpyHostToDevice, h->stream));
         SPH_CUDA(cudaMemcpyAsync(h->prev_c, prev, b, cudaMemcpyHostToDevice, h->stream));
-        SPH_CUDA(cudaMemcpyAsync(h->rho_c, rho, b, cudaMemcpyHostToDevice, h->stream));
+        SPH_CUDA(cudaMemcpyAsync(h->xr_c, xr, 2 * b, cudaMemcpyHostToDevice, h->stream));
     }
     SPH_CUDA(cudaMemsetAsync(h->d_state, 0, sizeof(DevState), h->stream));
     SPH_TRY(upload_soa_device(h, n));
@@ -217,7 +217,8 @@ static void free_all(sph_cuda *h)
 {
     destroy_graph(h);
     void *ptrs[] = {h->pos_a, h->vel_a, h->id_a, h->pos_b, h->prev_b, h->vel_b, h->kr_b,
-                    h->pos_c, h->prev_c, h->rho_c, h->id_c, h->tmp_id, h->cnt, h->start_a,
+                    h->pos_c, h->prev_c, h->xr_c, h->mask01_c, h->mask2_c, h->id_c,
+                    h->tmp_id, h->cnt, h->start_a,
                     h->start_c, h->tile_sums, h->d_params, h->d_state, h->d_partials,
                     h->d_scratch};
     for (void *p : ptrs)
@@ -305,7 +306,8 @@ int sph_cuda_create(sph_cuda_t **out, const param *params, const AABB_t *boundar
     if ((rc = dalloc(&h->pos_a, N)) || (rc = dalloc(&h->vel_a, N)) || (rc = dalloc(&h->id_a, N)) ||
         (rc = dalloc(&h->pos_b, N)) || (rc = dalloc(&h->prev_b, N)) ||
         (rc = dalloc(&h->vel_b, N)) || (rc = dalloc(&h->kr_b, N)) || (rc = dalloc(&h->pos_c, N)) ||
-        (rc = dalloc(&h->prev_c, N)) || (rc = dalloc(&h->rho_c, N)) || (rc = dalloc(&h->id_c, N)) ||
+        (rc = dalloc(&h->prev_c, N)) || (rc = dalloc(&h->xr_c, N)) ||
+        (rc = dalloc(&h->mask01_c, N)) || (rc = dalloc(&h->mask2_c, N)) || (rc = dalloc(&h->id_c, N)) ||
         (rc = dalloc(&h->tmp_id, N)) || (rc = dalloc(&h->cnt, C + 1 > N + 1 ? C + 1 : N + 1)) ||
         (rc = dalloc(&h->start_a, C + 2 > N + 1 ? C + 2 : N + 1)) ||
         (rc = dalloc(&h->start_c, C + 2)) || (rc = dalloc(&h->tile_sums, (size_t)h->ntiles)) ||
@@ -573,10 +575,11 @@ int sph_cuda_neighbor_lists(sph_cuda_t *h, int *counts, int *ids, long long max_
     const int n = h->n;
     *total = 0;
     if (n == 0) return SPH_OK;
-    // scratch: counts (n+1 words, scanned into offsets) | offsets (n+1) | ids
-    SPH_TRY(ensure_scratch(h, (size_t)(2 * n + 2) * sizeof(int) + 16));
+    // scratch: counts (n+1 words) | offsets (n+1 ints), each 256-byte aligned
+    const size_t part = (((size_t)(n + 1) * sizeof(int)) + 255) & ~(size_t)255;
+    SPH_TRY(ensure_scratch(h, 2 * part));
     unsigned *d_counts = (unsigned *)h->d_scratch;
-    int *d_off = (int *)(d_counts + n + 1);
+    int *d_off = (int *)((char *)h->d_scratch + part);
     SPH_CUDA(cudaMemsetAsync(d_counts, 0, (size_t)(n + 1) * sizeof(unsigned), h->stream));
     SPH_TRY(launch_half_lists(h, d_counts, d_off, nullptr, false));
     SPH_CUDA(cudaMemcpyAsync(counts, d_counts, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost,
@@ -613,14 +616,15 @@ static int probe(sph_cuda *h, const tunable_parameters *tp, int which, float *a,
         set_error("null output");
         return SPH_ERR_INVALID;
     }
-    SPH_TRY(ensure_scratch(h, (size_t)n * 3 * sizeof(float2) + 16));
+    const size_t sb = probe_scratch_bytes(n);
+    SPH_TRY(ensure_scratch(h, sb + (size_t)n * sizeof(float2) + 256));
     SPH_TRY(ensure_stage(h, (size_t)n * sizeof(float2) + 16));
-    float2 *t0 = (float2 *)h->d_scratch, *t1 = t0 + n, *out = t1 + n;
+    float2 *out = (float2 *)((char *)h->d_scratch + sb);
     // probes use their own parameters without disturbing the step's
     const tunable_parameters saved = h->last_tp;
     const bool had = h->tp_valid;
     SPH_TRY(set_params(h, tp));
-    SPH_TRY(launch_probe(h, which, t0, t1, out));
+    SPH_TRY(launch_probe(h, which, h->d_scratch, out));
     SPH_CUDA(cudaMemcpyAsync(h->h_stage, out, (size_t)n * sizeof(float2), cudaMemcpyDeviceToHost,
                              h->stream));
     if (had) SPH_TRY(set_params(h, &saved));
@@ -665,7 +669,6 @@ int sph_cuda_kernel_times(sph_cuda_t *h, const tunable_parameters *tp, float *ms
     for (int i = 0; i < ne; ++i) SPH_CUDA(cudaEventCreate(&ev[i]));
     int nk = 0;
     int rc = enqueue_step(h, ev, &nk);
-    enqueue_end_step(h);
     if (rc == SPH_OK) rc = cuda_fail(cudaEventSynchronize(ev[nk]), "timing sync");
     if (rc == SPH_OK) {
         for (int k = 0; k < nk && k < max; ++k) cudaEventElapsedTime(&ms[k], ev[k], ev[k + 1]);
@@ -680,7 +683,7 @@ const char *sph_cuda_kernel_name(int k) { return sph::kernel_name(k); }
 int sph_cuda_launches_per_step(sph_cuda_t *h)
 {
     if (!h) return 0;
-    return step_kernel_count() + 1;
+    return step_kernel_count();
 }
 
 int sph_cuda_timer_start(sph_cuda_t *h)

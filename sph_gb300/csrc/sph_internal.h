@@ -58,7 +58,10 @@ struct sph_cuda {
     int *id_a = nullptr;
     float2 *pos_b = nullptr, *prev_b = nullptr, *vel_b = nullptr;
     uint2 *kr_b = nullptr;  // (cell key, arrival rank) per particle
-    float2 *pos_c = nullptr, *prev_c = nullptr, *rho_c = nullptr;
+    float2 *pos_c = nullptr, *prev_c = nullptr;
+    float4 *xr_c = nullptr;               // (x, y, rho, rho_near) of the density pass
+    ulonglong2 *mask01_c = nullptr;       // neighbour hit masks of stencil rows 0, 1
+    unsigned long long *mask2_c = nullptr;  // ... and row 2
     int *id_c = nullptr;
     int *tmp_id = nullptr;
     unsigned int *cnt = nullptr;  // ncells + 1 counters, zero between builds
@@ -102,7 +105,7 @@ int cuda_fail(cudaError_t e, const char *what);
 // Core operations shared by the fast API and the legacy entry points.
 int ensure_scratch(sph_cuda *h, size_t bytes);
 int ensure_stage(sph_cuda *h, size_t bytes);
-int upload_soa_device(sph_cuda *h, int n);  // pos_b/vel_b (id order) + rho in rho_c -> state
+int upload_soa_device(sph_cuda *h, int n);  // pos_b/vel_b (id order) + xr_c -> state
 int set_params(sph_cuda *h, const tunable_parameters *tp);
 int enqueue_step(sph_cuda *h, cudaEvent_t *events, int *nkernels);
 int run_steps(sph_cuda *h, int nsteps);

@@ -224,9 +224,16 @@ __global__ void __launch_bounds__(kBlock)
 k_permute(int n, const uint2 *__restrict__ kr, const int *__restrict__ start,
           const int *__restrict__ tmp, const int *__restrict__ id_src,
           const float2 *__restrict__ a_src, const float2 *__restrict__ b_src,
-          int *__restrict__ id_dst, float2 *__restrict__ a_dst, float2 *__restrict__ b_dst)
+          int *__restrict__ id_dst, float2 *__restrict__ a_dst, float2 *__restrict__ b_dst,
+          DevState *__restrict__ end_step)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (end_step && i == 0) {
+        // last kernel of a step: the neighbour relation of the new positions
+        // now exists (viscosity is on from the next step), one more step done
+        end_step->lists_valid = 1u;
+        end_step->steps += 1ull;
+    }
     if (i >= n) return;
     const uint2 k = kr[i];
     const int s0 = __ldg(start + k.x), s1 = __ldg(start + k.x + 1);
@@ -296,7 +303,8 @@ k_viscosity_predict(int n, Grid g, const tunable_parameters *__restrict__ dP,
     const unsigned key = cell_key(p.x, p.y, g);
     if ((PROBE || st->lists_valid) && searchable(key, i, start, g, capped)) {
         for_each_candidate(key, start, g, capped, [&](int j) {
-            if (j == i) return;
+            // self (and any coincident particle) has r2 == 0: no impulse, as
+            // u is NaN in the reference for r == 0 (fluid.c:446-451)
             const float2 q = __ldg(pos + j);
             const float qx = q.x - p.x, qy = q.y - p.y;
             const float r2 = dist2(qx, qy);
@@ -334,13 +342,43 @@ k_viscosity_predict(int n, Grid g, const tunable_parameters *__restrict__ dP,
 // pass 2: density and near density (gather)
 // ---------------------------------------------------------------------------
 
+// The three stencil rows of a cell (slot 0: gy-1, 1: gy, 2: gy+1), each the
+// contiguous range [a[r], a[r] + len[r]) of sorted slots (empty outside the
+// grid).  Valid when no cell overflowed its bucket cap.
+__device__ __forceinline__ void stencil_rows(unsigned key, const int *__restrict__ start,
+                                             const Grid &g, int (&a)[3], int (&len)[3])
+{
+    const int gy = (int)(key / (unsigned)g.size_x);
+    const int gx = (int)key - gy * g.size_x;
+    const int x0 = gx > 0 ? gx - 1 : 0;
+    const int x1 = gx + 1 < g.size_x ? gx + 1 : g.size_x - 1;
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        const int y = gy + r - 1;
+        if (y < 0 || y >= g.size_y) {
+            a[r] = 0;
+            len[r] = 0;
+        } else {
+            const int row = y * g.size_x;
+            a[r] = __ldg(start + row + x0);
+            len[r] = __ldg(start + row + x1 + 1) - a[r];
+        }
+    }
+}
+
+constexpr int kMaskRow = 64;  // candidates per stencil row recorded in a hit mask
+
 // rho_i = sum_j (1 - r/h)^2, rho_near_i = sum_j (1 - r/h)^3 over neighbours
 // j != i with r/h < 1 (calculate_density, fluid.c:527-539; the pairs of
 // hash_fluid, hash.c:185/221: r2 <= h2 inclusive).
+// Writes xr = (x, y, rho, rho_near) and, per stencil row, the bit mask of the
+// candidates that are neighbours (r2 <= h2, self excluded), which the
+// relaxation pass of the same positions walks instead of the whole stencil.
 __global__ void __launch_bounds__(kBlock)
 k_density(int n, Grid g, const tunable_parameters *__restrict__ dP,
           const float2 *__restrict__ pos, const int *__restrict__ start,
-          const unsigned *__restrict__ occ_in, float2 *__restrict__ rho_out)
+          const unsigned *__restrict__ occ_in, float4 *__restrict__ xr_out,
+          ulonglong2 *__restrict__ mask01, unsigned long long *__restrict__ mask2)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -351,23 +389,57 @@ k_density(int n, Grid g, const tunable_parameters *__restrict__ dP,
     const float2 p = pos[i];
     const unsigned key = cell_key(p.x, p.y, g);
     float a = 0.0f, b = 0.0f;
+    unsigned long long m[3] = {0ull, 0ull, 0ull};
     if (searchable(key, i, start, g, capped)) {
-        for_each_candidate(key, start, g, capped, [&](int j) {
-            if (j == i) return;
-            const float2 q = __ldg(pos + j);
-            const float r2 = dist2(p.x - q.x, p.y - q.y);
-            if (r2 > h2) return;
-            const float r = r2 > 0.0f ? r2 * rsqrtf(r2) : 0.0f;
-            const float ratio = __fmul_rn(r, h_recip);
-            if (ratio < 1.0f) {
-                const float omr = 1.0f - ratio;
-                const float omr2 = omr * omr;
-                a += omr2;
-                b += omr2 * omr;
+        if (!capped) {
+            int ra[3], rl[3];
+            stencil_rows(key, start, g, ra, rl);
+#pragma unroll
+            for (int r = 0; r < 3; ++r) {
+                const float2 *row = pos + ra[r];
+                unsigned long long mr = 0ull;
+                for (int t = 0; t < rl[r]; ++t) {
+                    const float2 q = __ldg(row + t);
+                    const float r2 = dist2(p.x - q.x, p.y - q.y);
+                    if (r2 <= h2) {
+                        mr |= 1ull << (t & 63);
+                        const float rr = r2 > 0.0f ? r2 * rsqrtf(r2) : 0.0f;
+                        const float ratio = __fmul_rn(rr, h_recip);
+                        if (ratio < 1.0f) {
+                            const float omr = 1.0f - ratio;
+                            const float omr2 = omr * omr;
+                            a += omr2;
+                            b += omr2 * omr;
+                        }
+                    }
+                }
+                m[r] = mr;
             }
-        });
+            // the particle met itself (r = 0) in its own row: remove it
+            a -= 1.0f;
+            b -= 1.0f;
+            const int self = i - ra[1];
+            if (self < kMaskRow) m[1] &= ~(1ull << self);
+        } else {
+            for_each_candidate(key, start, g, true, [&](int j) {
+                if (j == i) return;
+                const float2 q = __ldg(pos + j);
+                const float r2 = dist2(p.x - q.x, p.y - q.y);
+                if (r2 > h2) return;
+                const float rr = r2 > 0.0f ? r2 * rsqrtf(r2) : 0.0f;
+                const float ratio = __fmul_rn(rr, h_recip);
+                if (ratio < 1.0f) {
+                    const float omr = 1.0f - ratio;
+                    const float omr2 = omr * omr;
+                    a += omr2;
+                    b += omr2 * omr;
+                }
+            });
+        }
     }
-    rho_out[i] = make_float2(a, b);
+    xr_out[i] = make_float4(p.x, p.y, a, b);
+    mask01[i] = make_ulonglong2(m[0], m[1]);
+    mask2[i] = m[2];
 }
 
 // ---------------------------------------------------------------------------
@@ -388,6 +460,38 @@ __device__ __noinline__ bool owns_pair(unsigned ki, int id_i, float2 qj, int id_
     return (dx == 0 && dy == 1) || (dx == 1 && dy >= -1 && dy <= 1);
 }
 
+struct RelaxConsts {
+    float h2, hh, h_recip, dt2, k, k_near, rest, half_spring;
+};
+
+// One neighbour's contribution to the displacement (r2 <= h2 known).
+__device__ __forceinline__ void relax_pair(const RelaxConsts &c, float2 p, float Pi, float Pni,
+                                           float4 q, int i, int j, unsigned key,
+                                           const int *__restrict__ ids, const Grid &g, float &ax,
+                                           float &ay, int &nudges)
+{
+    const float ex = p.x - q.x, ey = p.y - q.y;
+    const float r2 = dist2(ex, ey);
+    if (r2 <= 2e-12f) {
+        // r <= 1e-6 (rare): the owner of the pair is nudged (fluid.c:583-586)
+        const float r = r2 > 0.0f ? __fsqrt_rn(r2) : 0.0f;
+        if (j != i && r <= 0.000001f && owns_pair(key, ids[i], make_float2(q.x, q.y), ids[j], g))
+            ++nudges;
+        if (!(r > 0.0f)) return;
+    }
+    const float r_recip = rsqrtf(r2);
+    const float r = r2 * r_recip;
+    const float ratio = r * c.h_recip;
+    if (ratio < 1.0f) {
+        const float omr = 1.0f - ratio;
+        const float D = c.dt2 * ((Pi + c.k * (q.z - c.rest)) * omr +
+                                 (Pni + c.k_near * q.w) * omr * omr + c.half_spring * (c.hh - r));
+        const float s = D * r_recip;
+        ax += s * ex;
+        ay += s * ey;
+    }
+}
+
 // double_density_relaxation (fluid.c:541-611) in gather form:
 //   dx_i = sum_{j: 0 < r < h} D_ij (x_i - x_j)/r,
 //   D_ij = dt^2 [(P_i + P_j)(1 - r/h) + (Pn_i + Pn_j)(1 - r/h)^2 + k_spring (h - r)/2],
@@ -395,14 +499,17 @@ __device__ __noinline__ bool owns_pair(unsigned ki, int id_i, float2 qj, int id_
 // plus the reference's (1e-6, 1e-6) nudge for each pair with r <= 1e-6 that
 // the particle owns (fluid.c:583-586).  Then updateVelocities
 // (fluid.c:642-653): boundaryConditions, v = (x - x_prev)/dt clamped to +-5.
+// Walks the density pass's hit masks; rows longer than kMaskRow (or
+// overflowing buckets) fall back to the whole stencil.
 // PROBE writes the displacement instead of advancing.
 template <bool PROBE>
 __global__ void __launch_bounds__(kBlock)
 k_relax_update(int n, Grid g, const tunable_parameters *__restrict__ dP,
-               const float2 *__restrict__ pos, const float2 *__restrict__ rho,
-               const float2 *__restrict__ prev, const int *__restrict__ ids,
-               const int *__restrict__ start, const unsigned *__restrict__ occ_in,
-               unsigned *occ_reset, float2 *__restrict__ pos_out, float2 *__restrict__ vel_out,
+               const float4 *__restrict__ xr, const ulonglong2 *__restrict__ mask01,
+               const unsigned long long *__restrict__ mask2, const float2 *__restrict__ prev,
+               const int *__restrict__ ids, const int *__restrict__ start,
+               const unsigned *__restrict__ occ_in, unsigned *occ_reset,
+               float2 *__restrict__ pos_out, float2 *__restrict__ vel_out,
                uint2 *__restrict__ kr_out, unsigned *__restrict__ cnt,
                float2 *__restrict__ probe_out)
 {
@@ -410,47 +517,53 @@ k_relax_update(int n, Grid g, const tunable_parameters *__restrict__ dP,
     if (!PROBE && i == 0) *occ_reset = 0u;
     if (i >= n) return;
     const tunable_parameters P = *dP;
-    const float hh = P.smoothing_radius;
-    const float h2 = __fmul_rn(hh, hh);
-    const float h_recip = __fdiv_rn(1.0f, hh);
-    const float dt = P.time_step, dt2 = dt * dt;
-    const float k = P.k, k_near = P.k_near, rest = P.rest_density;
-    const float half_spring = 0.5f * P.k_spring;
+    RelaxConsts c;
+    c.hh = P.smoothing_radius;
+    c.h2 = __fmul_rn(c.hh, c.hh);
+    c.h_recip = __fdiv_rn(1.0f, c.hh);
+    const float dt = P.time_step;
+    c.dt2 = dt * dt;
+    c.k = P.k;
+    c.k_near = P.k_near;
+    c.rest = P.rest_density;
+    c.half_spring = 0.5f * P.k_spring;
     const bool capped = *occ_in > (unsigned)g.max_bucket;
 
-    const float2 p = pos[i];
-    const float2 rp = rho[i];
-    const float Pi = k * (rp.x - rest), Pni = k_near * rp.y;
+    const float4 me = xr[i];
+    const float2 p = make_float2(me.x, me.y);
+    const float Pi = c.k * (me.z - c.rest), Pni = c.k_near * me.w;
     const unsigned key = cell_key(p.x, p.y, g);
     float ax = 0.0f, ay = 0.0f;
     int nudges = 0;
     if (searchable(key, i, start, g, capped)) {
-        for_each_candidate(key, start, g, capped, [&](int j) {
-            if (j == i) return;
-            const float2 q = __ldg(pos + j);
-            const float ex = p.x - q.x, ey = p.y - q.y;
-            const float r2 = dist2(ex, ey);
-            if (r2 > h2) return;
-            if (r2 <= 1e-12f) {
-                // r <= 1e-6 (rare): the owner of the pair is nudged
-                const float r = r2 > 0.0f ? __fsqrt_rn(r2) : 0.0f;
-                if (r <= 0.000001f && owns_pair(key, ids[i], q, ids[j], g)) ++nudges;
-                if (!(r > 0.0f)) return;
+        bool walked = false;
+        if (!capped) {
+            int ra[3], rl[3];
+            stencil_rows(key, start, g, ra, rl);
+            if (rl[0] <= kMaskRow && rl[1] <= kMaskRow && rl[2] <= kMaskRow) {
+                const ulonglong2 m01 = mask01[i];
+                const unsigned long long mm[3] = {m01.x, m01.y, mask2[i]};
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+                    unsigned long long m = mm[r];
+                    while (m) {
+                        const int t = __ffsll((long long)m) - 1;
+                        m &= m - 1ull;
+                        const int j = ra[r] + t;
+                        relax_pair(c, p, Pi, Pni, __ldg(xr + j), i, j, key, ids, g, ax, ay, nudges);
+                    }
+                }
+                walked = true;
             }
-            const float r_recip = rsqrtf(r2);
-            const float r = r2 * r_recip;
-            const float ratio = r * h_recip;
-            if (ratio < 1.0f) {
-                const float2 rq = __ldg(rho + j);
-                const float omr = 1.0f - ratio;
-                const float D = dt2 * ((Pi + k * (rq.x - rest)) * omr +
-                                       (Pni + k_near * rq.y) * omr * omr +
-                                       half_spring * (hh - r));
-                const float s = D * r_recip;
-                ax += s * ex;
-                ay += s * ey;
-            }
-        });
+        }
+        if (!walked) {
+            for_each_candidate(key, start, g, capped, [&](int j) {
+                if (j == i) return;
+                const float4 q = __ldg(xr + j);
+                if (dist2(p.x - q.x, p.y - q.y) > c.h2) return;
+                relax_pair(c, p, Pi, Pni, q, i, j, key, ids, g, ax, ay, nudges);
+            });
+        }
     }
     const float nd = (float)nudges * 0.000001f;
     if (PROBE) {
@@ -479,7 +592,7 @@ __global__ void __launch_bounds__(kBlock)
 k_unpermute(int n, const tunable_parameters *__restrict__ dP, const int *__restrict__ id_a,
             const float2 *__restrict__ pos_a, const float2 *__restrict__ vel_a,
             const int *__restrict__ id_c, const float2 *__restrict__ prev_c,
-            const float2 *__restrict__ rho_c, float2 *__restrict__ out)
+            const float4 *__restrict__ xr_c, float2 *__restrict__ out)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -487,11 +600,22 @@ k_unpermute(int n, const tunable_parameters *__restrict__ dP, const int *__restr
     out[ia] = pos_a[i];
     out[(size_t)n + ia] = vel_a[i];
     out[2 * (size_t)n + ic] = prev_c[i];
-    const float2 r = rho_c[i];
+    const float4 x4 = xr_c[i];
+    const float2 r = make_float2(x4.z, x4.w);
     out[3 * (size_t)n + ic] = r;
     // pressure and near pressure, fluid.c:563-564
     out[4 * (size_t)n + ic] = make_float2(__fmul_rn(dP->k, __fsub_rn(r.x, dP->rest_density)),
                                           __fmul_rn(dP->k_near, r.y));
+}
+
+// (rho, rho_near) of the (x, y, rho, rho_near) records.
+__global__ void __launch_bounds__(kBlock)
+k_xr_density(int n, const float4 *__restrict__ xr, float2 *__restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 v = xr[i];
+    out[i] = make_float2(v.z, v.w);
 }
 
 // Sorted per-particle values -> id order.
@@ -527,16 +651,16 @@ k_pack_coords(int n, float max_x, float max_y, const int *__restrict__ id_a,
 
 // FP64 sums of density, near density and 0.5|v|^2, per block (fixed order).
 __global__ void __launch_bounds__(kBlock)
-k_diag_partial(int n, const float2 *__restrict__ rho_c, const float2 *__restrict__ vel_a,
+k_diag_partial(int n, const float4 *__restrict__ xr_c, const float2 *__restrict__ vel_a,
                double *__restrict__ partials)
 {
     __shared__ double sh[3][kBlock / 32];
     double a = 0.0, b = 0.0, c = 0.0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const float2 r = rho_c[i];
+        const float4 r = xr_c[i];
         const float2 v = vel_a[i];
-        a += r.x;
-        b += r.y;
+        a += r.z;
+        b += r.w;
         c += 0.5 * ((double)v.x * v.x + (double)v.y * v.y);
     }
     a = warp_sum(a); b = warp_sum(b); c = warp_sum(c);
@@ -615,14 +739,24 @@ k_half_lists(int n, Grid g, const tunable_parameters *__restrict__ dP,
 
 static inline int blocks_for(int n) { return (n + kBlock - 1) / kBlock; }
 
-// Exclusive scan of `in` (M entries) into out (M + 1 entries).
-static void launch_scan(sph_cuda *h, unsigned *in, int M, int *out, unsigned *occ, bool zero)
+// Exclusive scan of `in` (M entries) into out (M + 1 entries).  Both arrays
+// must be 16-byte aligned: the scan kernels move 16-byte vectors.
+static int launch_scan(sph_cuda *h, unsigned *in, int M, int *out, unsigned *occ, bool zero)
 {
+    if (((uintptr_t)in | (uintptr_t)out) & 15u) {
+        set_error("internal: scan arrays not 16-byte aligned");
+        return SPH_ERR_INVALID;
+    }
     const int tiles = (M + kScanTile - 1) / kScanTile;
+    if (tiles > h->ntiles) {
+        set_error("internal: scan of %d items exceeds the tile buffer", M);
+        return SPH_ERR_INVALID;
+    }
     k_scan_reduce<<<tiles, kScanThreads, 0, h->stream>>>(in, M, h->g.ncells, h->tile_sums,
                                                          h->d_state, occ, h->g.max_bucket,
                                                          h->g.max_neighbors);
     k_scan_apply<<<tiles, kScanThreads, 0, h->stream>>>(in, M, h->tile_sums, out, zero ? 1 : 0);
+    return SPH_OK;
 }
 
 static const char *const kKernelNames[] = {
@@ -659,13 +793,14 @@ int enqueue_step(sph_cuda *h, cudaEvent_t *events, int *nkernels)
     k_scatter_ids<<<nb, kBlock, 0, h->stream>>>(n, h->kr_b, h->id_a, h->start_c, h->tmp_id);
     mark();
     k_permute<<<nb, kBlock, 0, h->stream>>>(n, h->kr_b, h->start_c, h->tmp_id, h->id_a, h->pos_b,
-                                            h->prev_b, h->id_c, h->pos_c, h->prev_c);
+                                            h->prev_b, h->id_c, h->pos_c, h->prev_c, nullptr);
     mark();
     k_density<<<nb, kBlock, 0, h->stream>>>(n, h->g, h->d_params, h->pos_c, h->start_c,
-                                            &st->build_max_occ[SLOT_PREDICTED], h->rho_c);
+                                            &st->build_max_occ[SLOT_PREDICTED], h->xr_c,
+                                            h->mask01_c, h->mask2_c);
     mark();
     k_relax_update<false><<<nb, kBlock, 0, h->stream>>>(
-        n, h->g, h->d_params, h->pos_c, h->rho_c, h->prev_c, h->id_c, h->start_c,
+        n, h->g, h->d_params, h->xr_c, h->mask01_c, h->mask2_c, h->prev_c, h->id_c, h->start_c,
         &st->build_max_occ[SLOT_PREDICTED], &st->build_max_occ[SLOT_RELAXED], h->pos_b, h->vel_b,
         h->kr_b, h->cnt, nullptr);
     mark();
@@ -678,7 +813,7 @@ int enqueue_step(sph_cuda *h, cudaEvent_t *events, int *nkernels)
     k_scatter_ids<<<nb, kBlock, 0, h->stream>>>(n, h->kr_b, h->id_c, h->start_a, h->tmp_id);
     mark();
     k_permute<<<nb, kBlock, 0, h->stream>>>(n, h->kr_b, h->start_a, h->tmp_id, h->id_c, h->pos_b,
-                                            h->vel_b, h->id_a, h->pos_a, h->vel_a);
+                                            h->vel_b, h->id_a, h->pos_a, h->vel_a, st);
     mark();
     if (nkernels) *nkernels = e - 1;
     return cuda_fail(cudaGetLastError(), "step launch");
@@ -690,19 +825,8 @@ const char *kernel_name(int k)
 }
 int step_kernel_count() { return kStepKernels; }
 
-// Tail of every step (captured in the graph): lists now exist, step counter.
-__global__ void k_end_step(DevState *st)
-{
-    st->lists_valid = 1u;
-    st->steps += 1ull;
-}
 
-void enqueue_end_step(sph_cuda *h)
-{
-    k_end_step<<<1, 1, 0, h->stream>>>(h->d_state);
-}
-
-// Upload tail: pos_b / vel_b (id order) -> sorted A state; prev_c / rho_c
+// Upload tail: pos_b / vel_b (id order) -> sorted A state; prev_c / xr_c
 // already hold the uploaded values in id order.
 int upload_soa_device(sph_cuda *h, int n)
 {
@@ -712,10 +836,13 @@ int upload_soa_device(sph_cuda *h, int n)
         k_iota<<<nb, kBlock, 0, h->stream>>>(n, h->id_c);
         k_keys<<<nb, kBlock, 0, h->stream>>>(n, h->g, h->pos_b, h->kr_b, h->cnt,
                                              &st->build_max_occ[SLOT_RELAXED]);
-        launch_scan(h, h->cnt, h->g.ncells + 1, h->start_a, &st->build_max_occ[SLOT_RELAXED], true);
+        const int rc = launch_scan(h, h->cnt, h->g.ncells + 1, h->start_a,
+                                   &st->build_max_occ[SLOT_RELAXED], true);
+        if (rc != SPH_OK) return rc;
         k_scatter_ids<<<nb, kBlock, 0, h->stream>>>(n, h->kr_b, nullptr, h->start_a, h->tmp_id);
         k_permute<<<nb, kBlock, 0, h->stream>>>(n, h->kr_b, h->start_a, h->tmp_id, nullptr,
-                                                h->pos_b, h->vel_b, h->id_a, h->pos_a, h->vel_a);
+                                                h->pos_b, h->vel_b, h->id_a, h->pos_a, h->vel_a,
+                                                nullptr);
     }
     return cuda_fail(cudaGetLastError(), "upload kernels");
 }
@@ -724,7 +851,7 @@ int launch_unpermute(sph_cuda *h, float2 *out)
 {
     if (h->n == 0) return SPH_OK;
     k_unpermute<<<blocks_for(h->n), kBlock, 0, h->stream>>>(h->n, h->d_params, h->id_a, h->pos_a,
-                                                            h->vel_a, h->id_c, h->prev_c, h->rho_c,
+                                                            h->vel_a, h->id_c, h->prev_c, h->xr_c,
                                                             out);
     return cuda_fail(cudaGetLastError(), "unpermute");
 }
@@ -740,33 +867,48 @@ int launch_pack(sph_cuda *h, short2 *out)
 int launch_diagnostics(sph_cuda *h, double *d_out)
 {
     const int parts = h->npartials;
-    k_diag_partial<<<parts, kBlock, 0, h->stream>>>(h->n, h->rho_c, h->vel_a, h->d_partials);
+    k_diag_partial<<<parts, kBlock, 0, h->stream>>>(h->n, h->xr_c, h->vel_a, h->d_partials);
     k_diag_final<<<1, 32, 0, h->stream>>>(parts, h->n, h->d_partials, d_out);
     return cuda_fail(cudaGetLastError(), "diagnostics");
 }
 
 // Probes on the A state.  which: 0 density, 1 relaxation displacement,
-// 2 viscosity velocity change.  out: n float2 by id (device).
-int launch_probe(sph_cuda *h, int which, float2 *tmp_sorted, float2 *tmp_rho, float2 *out)
+// 2 viscosity velocity change.  `scratch` (probe_scratch_bytes(n), 256-byte
+// aligned) holds the sorted records; out: n float2 by id (device).
+size_t probe_scratch_bytes(int n)
+{
+    const size_t a = ((size_t)n * 16 + 255) & ~(size_t)255;
+    return 3 * a + (((size_t)n * 8 + 255) & ~(size_t)255);
+}
+
+int launch_probe(sph_cuda *h, int which, void *scratch, float2 *out)
 {
     const int n = h->n;
     if (n == 0) return SPH_OK;
     const int nb = blocks_for(n);
     DevState *st = h->d_state;
     const unsigned *occ = &st->build_max_occ[SLOT_RELAXED];
+    const size_t a = ((size_t)n * 16 + 255) & ~(size_t)255;
+    char *base = (char *)scratch;
+    float4 *xr = (float4 *)base;
+    ulonglong2 *m01 = (ulonglong2 *)(base + a);
+    unsigned long long *m2 = (unsigned long long *)(base + 2 * a);
+    float2 *sorted = (float2 *)(base + 3 * a);
     if (which == 0 || which == 1) {
-        k_density<<<nb, kBlock, 0, h->stream>>>(n, h->g, h->d_params, h->pos_a, h->start_a, occ,
-                                                which == 0 ? tmp_sorted : tmp_rho);
+        k_density<<<nb, kBlock, 0, h->stream>>>(n, h->g, h->d_params, h->pos_a, h->start_a, occ, xr,
+                                                m01, m2);
         if (which == 1)
             k_relax_update<true><<<nb, kBlock, 0, h->stream>>>(
-                n, h->g, h->d_params, h->pos_a, tmp_rho, nullptr, h->id_a, h->start_a, occ,
-                nullptr, nullptr, nullptr, nullptr, nullptr, tmp_sorted);
+                n, h->g, h->d_params, xr, m01, m2, nullptr, h->id_a, h->start_a, occ, nullptr,
+                nullptr, nullptr, nullptr, nullptr, sorted);
+        else
+            k_xr_density<<<nb, kBlock, 0, h->stream>>>(n, xr, sorted);
     } else {
         k_viscosity_predict<true><<<nb, kBlock, 0, h->stream>>>(
             n, h->g, h->d_params, st, h->pos_a, h->vel_a, h->start_a, occ, nullptr, nullptr,
-            nullptr, nullptr, nullptr, tmp_sorted);
+            nullptr, nullptr, nullptr, sorted);
     }
-    k_by_id<<<nb, kBlock, 0, h->stream>>>(n, h->id_a, tmp_sorted, out);
+    k_by_id<<<nb, kBlock, 0, h->stream>>>(n, h->id_a, sorted, out);
     return cuda_fail(cudaGetLastError(), "probe");
 }
 
@@ -782,7 +924,8 @@ int launch_half_lists(sph_cuda *h, unsigned *d_counts, int *d_off, int *d_ids, b
         k_half_lists<false><<<nb, kBlock, 0, h->stream>>>(n, h->g, h->d_params, h->pos_a, h->id_a,
                                                           h->start_a, occ, d_counts, nullptr,
                                                           nullptr);
-        launch_scan(h, d_counts, n, d_off, nullptr, false);
+        const int rc = launch_scan(h, d_counts, n, d_off, nullptr, false);
+        if (rc != SPH_OK) return rc;
     } else {
         k_half_lists<true><<<nb, kBlock, 0, h->stream>>>(n, h->g, h->d_params, h->pos_a, h->id_a,
                                                          h->start_a, occ, nullptr, d_off, d_ids);

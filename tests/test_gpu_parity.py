@@ -186,14 +186,30 @@ def test_mover_steps_match_cpu_jacobi(cuda_lib, tag):
     P, C = sc.params.as_dict(), sc.config()
     mv = sc.mover_schedule(0, 20)
     orc = oracle.Sim("port", sc.x, sc.y, sc.vx, sc.vy, P, C)
-    od = orc.step(20, mv, jacobi=True)
     with Simulation.from_scene(sc) as s:
-        s.step_schedule([sc.params_at(t).as_dict() for t in range(20)])
-        a = s.download()
+        # the two gathers differ only in summation order: tight after 3 steps
+        s.step_schedule([sc.params_at(t).as_dict() for t in range(3)])
+        orc.step(3, mv[:3], jacobi=True)
+        a, b = s.download(), orc.get()
+        for k in ("x", "y"):
+            assert np.abs(a[k] - b[k]).max() < 1e-4, (k, np.abs(a[k] - b[k]).max())
+        # the stirred fluid amplifies rounding differences: bound the bulk and
+        # the diagnostics after 20 steps
+        s.step_schedule([sc.params_at(t).as_dict() for t in range(3, 20)])
+        od = orc.step(17, mv[3:], jacobi=True)
+        a, b = s.download(), orc.get()
         gd = s.diagnostics()
-    b = orc.get()
-    assert np.abs(a["x"] - b["x"]).max() < 1e-3 and np.abs(a["y"] - b["y"]).max() < 1e-3
+    for k in ("x", "y"):
+        err = np.abs(a[k] - b[k])
+        assert np.percentile(err, 99) < 1e-4 and err.max() < 1e-2, (k, np.percentile(err, 99), err.max())
     assert np.allclose(gd, od[-1], rtol=1e-3)
+    # boundaryConditions ran last in the step: no particle is inside the mover
+    cx, cy = mv[-1]
+    if tag == "sphere":
+        assert np.hypot(a["x"] - cx, a["y"] - cy).min() >= 8.0 - 1e-3
+    else:
+        inside = (np.abs(a["x"] - cx) < 6.0 - 1e-3) & (np.abs(a["y"] - cy) < 3.0 - 1e-3)
+        assert not inside.any()
 
 
 def test_rebuild_neighbors_enables_first_step_viscosity(cuda_lib):
@@ -311,5 +327,5 @@ def test_kernel_times(cuda_lib):
     with Simulation.from_scene(sc) as s:
         s.step(P, 3)
         times = s.kernel_times(P)
-        assert s.launches_per_step() == 12
+        assert s.launches_per_step() == 11
     assert len(times) == 11 and all(v > 0 for v in times.values())
