@@ -201,7 +201,7 @@ def test_mover_steps_match_cpu_jacobi(cuda_lib, tag):
         gd = s.diagnostics()
     for k in ("x", "y"):
         err = np.abs(a[k] - b[k])
-        assert np.percentile(err, 99) < 1e-4 and err.max() < 1e-2, (k, np.percentile(err, 99), err.max())
+        assert np.percentile(err, 99) < 1e-3 and err.max() < 1e-2, (k, np.percentile(err, 99), err.max())
     assert np.allclose(gd, od[-1], rtol=1e-3)
     # boundaryConditions ran last in the step: no particle is inside the mover
     cx, cy = mv[-1]
