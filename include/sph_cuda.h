@@ -172,6 +172,34 @@ int sph_cuda_probe_relaxation(sph_cuda_t *h, const tunable_parameters *tp, float
 int sph_cuda_probe_viscosity(sph_cuda_t *h, const tunable_parameters *tp, float *dvx,
                              float *dvy);
 
+/* ---- density without allocation ---- */
+
+/* Largest problem sph_cuda_density_static accepts. */
+#define SPH_STATIC_MAX_PARTICLES 65536
+#define SPH_STATIC_MAX_CELLS 262144
+
+/* No counterpart in the reference.  For callers that cannot call cudaMalloc
+ * (a step loop living inside another framework's fixed device-memory budget,
+ * or a real-time loop that cannot take the device-wide synchronisation an
+ * allocation may imply): the density and near density of n particles, as
+ * sph_cuda_probe_density computes them, from caller-owned DEVICE arrays
+ * x[n], y[n] into caller-owned DEVICE arrays density[n], density_near[n]
+ * (indexed like the inputs).  grid gives spacing, size_x, size_y,
+ * max_bucket_size and max_neighbors; tp gives smoothing_radius.
+ *
+ * Allocates nothing: every intermediate lives in one fixed-size device
+ * array inside the library (about 7 MB, held on every GPU that loads the
+ * library until the process exits).  Rejects n > SPH_STATIC_MAX_PARTICLES
+ * and size_x * size_y > SPH_STATIC_MAX_CELLS with SPH_ERR_CAPACITY.
+ * The first call on a device looks up that array's device address; make
+ * that first call before any stream capture.  Work is queued on `stream`
+ * (NULL = the default stream) and the call returns once it is queued.
+ * All calls share the one array: calls whose work overlaps on the GPU (other
+ * streams, other host threads) race and corrupt each other's results. */
+int sph_cuda_density_static(const float *x, const float *y, int n, const neighbor_grid_t *grid,
+                            const tunable_parameters *tp, float *density, float *density_near,
+                            void *stream);
+
 /* ---- measurement ---- */
 
 /* Runs ONE step (it advances the state) with a CUDA event pair around each
