@@ -112,4 +112,30 @@ __device__ __forceinline__ bool searchable(unsigned key, int slot, const int *__
     return !capped || slot - __ldg(start + key) < g.max_bucket;
 }
 
+// The three stencil rows of a cell (slot 0: gy-1, 1: gy, 2: gy+1), each the
+// contiguous range [a[r], a[r] + len[r]) of sorted slots (empty outside the
+// grid).  Valid when no cell overflowed its bucket cap.
+__device__ __forceinline__ void stencil_rows(unsigned key, const int *__restrict__ start,
+                                             const Grid &g, int (&a)[3], int (&len)[3])
+{
+    const int gy = (int)(key / (unsigned)g.size_x);
+    const int gx = (int)key - gy * g.size_x;
+    const int x0 = gx > 0 ? gx - 1 : 0;
+    const int x1 = gx + 1 < g.size_x ? gx + 1 : g.size_x - 1;
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        const int y = gy + r - 1;
+        if (y < 0 || y >= g.size_y) {
+            a[r] = 0;
+            len[r] = 0;
+        } else {
+            const int row = y * g.size_x;
+            a[r] = __ldg(start + row + x0);
+            len[r] = __ldg(start + row + x1 + 1) - a[r];
+        }
+    }
+}
+
+constexpr int kMaskRow = 64;  // candidates per stencil row recorded in a hit mask
+
 }  // namespace sph

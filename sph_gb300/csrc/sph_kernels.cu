@@ -301,26 +301,63 @@ k_viscosity_predict(int n, Grid g, const tunable_parameters *__restrict__ dP,
     v.y = __fadd_rn(v.y, gdt);
     float dvx = 0.0f, dvy = 0.0f;
     const unsigned key = cell_key(p.x, p.y, g);
+    // One pair's impulse on this particle; self (and any coincident
+    // particle) has r2 == 0 and gives none, as u is NaN in the reference for
+    // r == 0 (fluid.c:446-451).
+    auto impulse = [&](int j) {
+        const float2 q = __ldg(pos + j);
+        const float qx = q.x - p.x, qy = q.y - p.y;
+        const float r2 = dist2(qx, qy);
+        if (r2 > h2 || r2 == 0.0f) return;
+        float2 w = __ldg(vel + j);
+        w.y = __fadd_rn(w.y, gdt);
+        const float r_recip = rsqrtf(r2);
+        const float r = r2 * r_recip;
+        const float u = ((v.x - w.x) * qx + (v.y - w.y) * qy) * r_recip;
+        if (u > 0.0f) {
+            const float ratio = r * h_recip;
+            const float imp = dt * (1.0f - ratio) * (sigma * u + beta * u * u);
+            dvx -= 0.5f * clamp5(imp * qx * r_recip);
+            dvy -= 0.5f * clamp5(imp * qy * r_recip);
+        }
+    };
     if ((PROBE || st->lists_valid) && searchable(key, i, start, g, capped)) {
-        for_each_candidate(key, start, g, capped, [&](int j) {
-            // self (and any coincident particle) has r2 == 0: no impulse, as
-            // u is NaN in the reference for r == 0 (fluid.c:446-451)
-            const float2 q = __ldg(pos + j);
-            const float qx = q.x - p.x, qy = q.y - p.y;
-            const float r2 = dist2(qx, qy);
-            if (r2 > h2 || r2 == 0.0f) return;
-            float2 w = __ldg(vel + j);
-            w.y = __fadd_rn(w.y, gdt);
-            const float r_recip = rsqrtf(r2);
-            const float r = r2 * r_recip;
-            const float u = ((v.x - w.x) * qx + (v.y - w.y) * qy) * r_recip;
-            if (u > 0.0f) {
-                const float ratio = r * h_recip;
-                const float imp = dt * (1.0f - ratio) * (sigma * u + beta * u * u);
-                dvx -= 0.5f * clamp5(imp * qx * r_recip);
-                dvy -= 0.5f * clamp5(imp * qy * r_recip);
+        bool walked = false;
+        if (!capped) {
+            // two phases: a cheap scan marks the neighbours of each stencil
+            // row, then only they pay for the impulse (less SIMT waste)
+            int ra[3], rl[3];
+            stencil_rows(key, start, g, ra, rl);
+            if (rl[0] <= kMaskRow && rl[1] <= kMaskRow && rl[2] <= kMaskRow) {
+                unsigned long long m[3];
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+                    const float2 *row = pos + ra[r];
+                    unsigned long long mr = 0ull;
+#pragma unroll 4
+                    for (int t = 0; t < rl[r]; ++t) {
+                        const float2 q = __ldg(row + t);
+                        const float r2 = dist2(q.x - p.x, q.y - p.y);
+                        // self and coincident particles are marked too; the
+                        // impulse skips them (r2 == 0)
+                        mr |= (unsigned long long)(r2 <= h2) << t;
+                    }
+                    m[r] = mr;
+                }
+                m[1] &= ~(1ull << (i - ra[1]));  // self
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+                    unsigned long long mr = m[r];
+                    while (mr) {
+                        const int t = __ffsll((long long)mr) - 1;
+                        mr &= mr - 1ull;
+                        impulse(ra[r] + t);
+                    }
+                }
+                walked = true;
             }
-        });
+        }
+        if (!walked) for_each_candidate(key, start, g, capped, impulse);
     }
     if (PROBE) {
         probe_out[i] = make_float2(dvx, dvy);
@@ -341,32 +378,6 @@ k_viscosity_predict(int n, Grid g, const tunable_parameters *__restrict__ dP,
 // ---------------------------------------------------------------------------
 // pass 2: density and near density (gather)
 // ---------------------------------------------------------------------------
-
-// The three stencil rows of a cell (slot 0: gy-1, 1: gy, 2: gy+1), each the
-// contiguous range [a[r], a[r] + len[r]) of sorted slots (empty outside the
-// grid).  Valid when no cell overflowed its bucket cap.
-__device__ __forceinline__ void stencil_rows(unsigned key, const int *__restrict__ start,
-                                             const Grid &g, int (&a)[3], int (&len)[3])
-{
-    const int gy = (int)(key / (unsigned)g.size_x);
-    const int gx = (int)key - gy * g.size_x;
-    const int x0 = gx > 0 ? gx - 1 : 0;
-    const int x1 = gx + 1 < g.size_x ? gx + 1 : g.size_x - 1;
-#pragma unroll
-    for (int r = 0; r < 3; ++r) {
-        const int y = gy + r - 1;
-        if (y < 0 || y >= g.size_y) {
-            a[r] = 0;
-            len[r] = 0;
-        } else {
-            const int row = y * g.size_x;
-            a[r] = __ldg(start + row + x0);
-            len[r] = __ldg(start + row + x1 + 1) - a[r];
-        }
-    }
-}
-
-constexpr int kMaskRow = 64;  // candidates per stencil row recorded in a hit mask
 
 // rho_i = sum_j (1 - r/h)^2, rho_near_i = sum_j (1 - r/h)^3 over neighbours
 // j != i with r/h < 1 (calculate_density, fluid.c:527-539; the pairs of
@@ -398,6 +409,7 @@ k_density(int n, Grid g, const tunable_parameters *__restrict__ dP,
             for (int r = 0; r < 3; ++r) {
                 const float2 *row = pos + ra[r];
                 unsigned long long mr = 0ull;
+#pragma unroll 4
                 for (int t = 0; t < rl[r]; ++t) {
                     const float2 q = __ldg(row + t);
                     const float r2 = dist2(p.x - q.x, p.y - q.y);
@@ -503,7 +515,7 @@ __device__ __forceinline__ void relax_pair(const RelaxConsts &c, float2 p, float
 // overflowing buckets) fall back to the whole stencil.
 // PROBE writes the displacement instead of advancing.
 template <bool PROBE>
-__global__ void __launch_bounds__(kBlock)
+__global__ void __launch_bounds__(kBlock, 5)
 k_relax_update(int n, Grid g, const tunable_parameters *__restrict__ dP,
                const float4 *__restrict__ xr, const ulonglong2 *__restrict__ mask01,
                const unsigned long long *__restrict__ mask2, const float2 *__restrict__ prev,
