@@ -10,7 +10,7 @@ from sph_gb300 import _lib
 
 def test_library_exports_every_declared_symbol(cuda_lib):
     declared = _lib.declared_symbols()
-    assert "sph_cuda_step" in declared
+    assert "sph_cuda_step" in declared and "hash_fluid" in declared
     missing = [s for s in declared if not hasattr(cuda_lib, s)]
     assert not missing, missing
 
