@@ -251,25 +251,105 @@ def traffic_per_launch(kernel: str, n: int):
         return None
 
 
+class DamBreak:
+    """The 4,194,304-particle dam break with the moving sphere mover."""
+
+    def __init__(self, n):
+        from sph_gb300 import scenes
+        self.sc = scenes.config2(n=n)
+        self.n, self.cells = self.sc.n, self.sc.cells
+        self.name = (f"dam break, {self.n} particles, box {self.sc.box[1]:g}h x {self.sc.box[3]:g}h, "
+                     f"moving sphere mover r=8h, plain method")
+        self.params = {}
+
+    def p(self, t):
+        if t not in self.params:
+            self.params[t] = self.sc.params_at(t).as_dict()
+        return self.params[t]
+
+    def fresh(self):
+        from sph_gb300 import Simulation
+        return Simulation.from_scene(self.sc)
+
+    def advance(self, sim, t0, k):
+        sim.step_schedule([self.p(t) for t in range(t0, t0 + k)])
+
+    def step_one(self, sim, t):
+        sim.step(self.p(t))
+
+    def tune(self, sim, t0):
+        shapes = sim.autotune(1)  # 8 steps with the tunables of step t0 - 1
+        return t0 + 8, shapes
+
+    def cpu_sample(self, args):
+        return cpu_baseline_single(args.cpu_sample, args.cpu_steps)
+
+
+class EnsembleWork:
+    """512 independent scenes of 1,024-65,536 particles in one step."""
+
+    def __init__(self, nscenes):
+        from sph_gb300 import scenes
+        self.scs = scenes.config3(nscenes)
+        self.n = sum(s.n for s in self.scs)
+        self.cells = sum(s.cells for s in self.scs)
+        self.name = (f"batched ensemble, {nscenes} scenes, {self.n} particles (1,024-65,536 per "
+                     f"scene, log-uniform), plain method")
+
+    def fresh(self):
+        from sph_gb300 import Ensemble
+        e = Ensemble(self.scs)
+        e.upload_scenes()
+        return e
+
+    def advance(self, sim, t0, k):
+        sim.step(None, k)
+
+    def step_one(self, sim, t):
+        sim.step(None, 1)
+
+    def tune(self, sim, t0):
+        shapes = sim.autotune(2)  # 16 steps, part of the warm-up
+        return t0 + 16, shapes
+
+    def cpu_sample(self, args):
+        import oracle
+        kind, label = cpu_kind()
+        sample = self.scs[:16]
+        steps = max(2, args.cpu_steps // 2)
+        total = 0.0
+        for sc in sample:
+            sim = oracle.Sim(kind, sc.x, sc.y, sc.vx, sc.vy, sc.params.as_dict(), sc.config())
+            sim.step(1)
+            t0 = time.perf_counter()
+            sim.step(steps)
+            total += time.perf_counter() - t0
+            sim.close()
+        np_ = sum(s.n for s in sample)
+        return {"value": np_ * steps / total, "unit": "particle-steps/s", "cores": 1, "kind": label,
+                "sample": f"the first 16 scenes of the ensemble ({np_} particles), {steps} steps each "
+                          f"after one untimed step, reference step order, single thread"}
+
+
 def run_gpu(args, world, rank):
     import numpy as np
 
-    from sph_gb300 import Simulation, scenes
+    from sph_gb300 import scenes
     from sph_gb300.simulation import PinnedArray
 
-    sc = scenes.config2(n=args.n)
-    n, cells = sc.n, sc.cells
+    work = EnsembleWork(args.scenes) if args.workload == "ensemble" else DamBreak(args.n)
+    n, cells = work.n, work.cells
     K, W = args.steps, args.warmup
-    params = [sc.params_at(t).as_dict() for t in range(W + K)]
 
     # ---- device-resident throughput ----
-    sim = Simulation.from_scene(sc)
-    sim.step_schedule(params[:W])
+    sim = work.fresh()
+    work.advance(sim, 0, W)
+    t0, shapes = work.tune(sim, W)
     sim.synchronize()
     barrier(world)
     with ClockSampler(0) as clk:
         sim.timer_start()
-        sim.step_schedule(params[W:W + K])
+        work.advance(sim, t0, K)
         ms = sim.timer_stop()
     clocks = clk.summary()
     ms = max_over_ranks(world, ms)
@@ -280,7 +360,7 @@ def run_gpu(args, world, rank):
     counters = sim.counters()
 
     # ---- per-kernel times (CUDA events on the library stream) ----
-    kt_runs = [sim.kernel_times(params[min(W + K + i, W + K - 1)]) for i in range(5)]
+    kt_runs = [sim.kernel_times(None) for _ in range(5)]
     ktimes = {k: statistics.median(r[k] for r in kt_runs) for k in kt_runs[0]}
     sim.close()
     top = max(ktimes, key=ktimes.get)
@@ -301,13 +381,12 @@ def run_gpu(args, world, rank):
     e2e = None
     if not args.no_e2e:
         coords = PinnedArray((n, 2), np.int16)
-        t0 = time.perf_counter()
-        sim2 = Simulation(sc.params.as_dict(), sc.config(), n)
-        sim2.upload(sc.x, sc.y, sc.vx, sc.vy)
+        tw = time.perf_counter()
+        sim2 = work.fresh()
         for t in range(W + K):
-            sim2.step(params[t])
+            work.step_one(sim2, t)
             sim2.pack_coords(coords.array)
-        t_e2e = time.perf_counter() - t0
+        t_e2e = time.perf_counter() - tw
         sim2.close()
         coords.free()
         t_e2e = max_over_ranks(world, t_e2e)
@@ -318,18 +397,17 @@ def run_gpu(args, world, rank):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_baseline_single(args.cpu_sample, args.cpu_steps)
+        cpu = work.cpu_sample(args)
 
     if rank == 0:
         line = {"metric": "particle-steps/s", "value": value, "unit": "particle-steps/s",
                 "n_gpus": world, "steps": K, "warmup": W, "ms_per_step": ms / K,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32", "data": "synthetic",
-                "config": {"workload": f"dam break, {n} particles, box {sc.box[1]:g}h x {sc.box[3]:g}h, "
-                                       f"moving sphere mover r=8h, plain method",
+                "config": {"workload": work.name,
                            "particles": n, "cells": cells, "parallelism": f"replicas x{world}",
                            "l2": "no flush: per-step working set ~0.5 GB > 129 MB L2",
-                           "steps_timed": f"{W}..{W + K - 1}"},
+                           "steps_timed": f"{t0}..{t0 + K - 1}", "launch_shapes": shapes},
                 "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
                 "clocks": clocks, "gpu_launches": launches,
                 "diagnostics": {"mean_density": diag[0], "mean_near_density": diag[1],
@@ -345,6 +423,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=4_194_304)
+    ap.add_argument("--workload", default="dam_break", choices=["dam_break", "ensemble"])
+    ap.add_argument("--scenes", type=int, default=512)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=262_144)

@@ -77,6 +77,49 @@ typedef struct sph_cuda_counters {
 int sph_cuda_create(sph_cuda_t **out, const param *params, const AABB_t *boundary,
                     const neighbor_grid_t *grid, int max_particles);
 
+/* One scene of an ensemble: an independent domain, as one compute rank's
+ * set-up would describe it (fluid.c:88-176, 214-215). */
+typedef struct sph_scene_desc {
+    tunable_parameters params;   /* the scene's tunables (smoothing_radius = its h) */
+    AABB_t boundary;             /* its box */
+    float spacing;               /* its neighbour-grid spacing */
+    unsigned int size_x, size_y; /* its grid dimensions */
+    int n;                       /* its particle count */
+} sph_scene_desc;
+
+/* No counterpart in the reference (one rank runs one domain there).  Creates
+ * a handle holding `nscenes` independent scenes that advance together: every
+ * kernel of a step covers the particles of all scenes, each particle using
+ * its own scene's grid and tunables.  Particles are uploaded and downloaded
+ * concatenated in scene order (scene s holds ids [sum of n of scenes < s,
+ * + n_s)); uploads must pass exactly the total count.  max_bucket and
+ * max_neighbors apply to every scene.  Each scene's trajectory is identical,
+ * bit for bit, to that scene run alone. */
+int sph_cuda_create_ensemble(sph_cuda_t **out, const sph_scene_desc *scenes, int nscenes,
+                             int max_bucket, int max_neighbors);
+
+/* Sets scene `scene`'s tunables for the following steps (all handles). */
+int sph_cuda_set_scene_params(sph_cuda_t *h, int scene, const tunable_parameters *tp);
+
+/* Number of scenes of the handle (1 for sph_cuda_create). */
+int sph_cuda_num_scenes(sph_cuda_t *h);
+
+/* FP64 mean density, mean near density and kinetic energy per particle of
+ * every scene: out[3 s + 0..2]. */
+int sph_cuda_scene_diagnostics(sph_cuda_t *h, double *out);
+
+/* Launch shapes of the three gather kernels (viscosity_predict, density,
+ * relax_update): shapes[2k] threads per block, shapes[2k+1] 0 for one block
+ * per tile of particles or the number of resident blocks per SM for a
+ * persistent grid-stride launch.  Any shape gives the same results. */
+int sph_cuda_set_launch_shapes(sph_cuda_t *h, const int *shapes);
+int sph_cuda_get_launch_shapes(sph_cuda_t *h, int *shapes);
+
+/* Autotuner: times every candidate shape on the three gathers for
+ * trial_steps steps each (the steps advance the simulation) and keeps the
+ * fastest per gather; the chosen shapes go to shapes_out (6 ints) if given. */
+int sph_cuda_autotune(sph_cuda_t *h, int trial_steps, int *shapes_out);
+
 /* Frees all device and host resources of the handle. */
 int sph_cuda_destroy(sph_cuda_t *h);
 
@@ -98,15 +141,15 @@ int sph_cuda_upload_particles(sph_cuda_t *h, const fluid_particle *particles, in
 int sph_cuda_upload_soa(sph_cuda_t *h, const float *x, const float *y, const float *vx,
                         const float *vy, int n);
 
-/* Runs nsteps steps with the given tunables (copied at call time).  Each step
- * is the reference sequence fluid.c:273-348: apply_gravity,
- * viscosity_impluses, predict_positions, hash_fluid(.., true),
- * double_density_relaxation, updateVelocities, hash_fluid(.., false) --
- * with viscosity and relaxation as deterministic gathers (Jacobi form).
- * Captured as one CUDA graph per step. */
+/* Runs nsteps steps with the given tunables (copied at call time; NULL keeps
+ * the current ones, and an ensemble takes NULL).  Each step is the reference
+ * sequence fluid.c:273-348: apply_gravity, viscosity_impluses,
+ * predict_positions, hash_fluid(.., true), double_density_relaxation,
+ * updateVelocities, hash_fluid(.., false) -- with viscosity and relaxation as
+ * deterministic gathers (Jacobi form).  Captured as one CUDA graph per step. */
 int sph_cuda_step(sph_cuda_t *h, const tunable_parameters *tp, int nsteps);
 
-/* Runs nsteps steps, step t using tps[t] (e.g. a moving mover). */
+/* Runs nsteps steps, step t using tps[t] (e.g. a moving mover); single scene. */
 int sph_cuda_step_schedule(sph_cuda_t *h, const tunable_parameters *tps, int nsteps);
 
 /* Writes the particle state back through the caller's pointer array:

@@ -6,6 +6,6 @@ wraps it for Python callers; it contains no CPU implementation of the step.
 """
 from . import scenes
 from ._lib import PARTICLE_DTYPE, SphError, lib
-from .simulation import Simulation
+from .simulation import Ensemble, Simulation
 
-__all__ = ["Simulation", "SphError", "PARTICLE_DTYPE", "scenes", "lib"]
+__all__ = ["Simulation", "Ensemble", "SphError", "PARTICLE_DTYPE", "scenes", "lib"]

@@ -74,6 +74,12 @@ class NeighborGrid(ctypes.Structure):
                 ("max_neighbors", ctypes.c_uint), ("max_bucket_size", ctypes.c_uint)]
 
 
+class SceneDesc(ctypes.Structure):
+    """sph_scene_desc (include/sph_cuda.h): one scene of an ensemble."""
+    _fields_ = [("params", TunableParameters), ("boundary", AABB), ("spacing", ctypes.c_float),
+                ("size_x", ctypes.c_uint), ("size_y", ctypes.c_uint), ("n", ctypes.c_int)]
+
+
 class Counters(ctypes.Structure):
     _fields_ = [("steps", ctypes.c_ulonglong), ("out_of_grid", ctypes.c_ulonglong),
                 ("bucket_overflow", ctypes.c_ulonglong), ("max_cell_occupancy", ctypes.c_uint),
@@ -97,6 +103,14 @@ _SIGS = {
     "sph_cuda_create": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.POINTER(Param), ctypes.POINTER(AABB),
                                        ctypes.POINTER(NeighborGrid), ctypes.c_int]),
     "sph_cuda_destroy": (ctypes.c_int, [_P]),
+    "sph_cuda_create_ensemble": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.POINTER(SceneDesc), ctypes.c_int,
+                                                ctypes.c_int, ctypes.c_int]),
+    "sph_cuda_set_scene_params": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(TunableParameters)]),
+    "sph_cuda_num_scenes": (ctypes.c_int, [_P]),
+    "sph_cuda_scene_diagnostics": (ctypes.c_int, [_P, c_double_p]),
+    "sph_cuda_set_launch_shapes": (ctypes.c_int, [_P, c_int_p]),
+    "sph_cuda_get_launch_shapes": (ctypes.c_int, [_P, c_int_p]),
+    "sph_cuda_autotune": (ctypes.c_int, [_P, ctypes.c_int, c_int_p]),
     "sph_cuda_set_stream": (ctypes.c_int, [_P, _P]),
     "sph_cuda_upload": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.POINTER(FluidParticle)), ctypes.c_int]),
     "sph_cuda_upload_particles": (ctypes.c_int, [_P, _P, ctypes.c_int]),

@@ -1,4 +1,5 @@
 // sph_capi.cu -- handle lifecycle and the device-resident C API of libsph_cuda.
+#include <algorithm>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
@@ -13,6 +14,7 @@ namespace sph {
 int launch_unpermute(sph_cuda *h, float2 *out);
 int launch_pack(sph_cuda *h, short2 *out);
 int launch_diagnostics(sph_cuda *h, double *d_out);
+int launch_scene_diagnostics(sph_cuda *h, double *d_out);
 int launch_probe(sph_cuda *h, int which, void *scratch, float2 *out);
 size_t probe_scratch_bytes(int n);
 int launch_half_lists(sph_cuda *h, unsigned *d_counts, int *d_off, int *d_ids, bool write);
@@ -103,21 +105,22 @@ static int capture_step(sph_cuda *h)
     return SPH_OK;
 }
 
-// Copies the tunables into the device parameter block through a pinned
-// ring slot, so that the copy is asynchronous and the caller's struct can be
-// reused at once.  Skipped when unchanged.
-int set_params(sph_cuda *h, const tunable_parameters *tp)
+// Copies a scene's tunables into its record of the device scene table
+// through a pinned ring slot, so that the copy is asynchronous and the
+// caller's struct can be reused at once.  Skipped when unchanged.
+int set_scene_params(sph_cuda *h, int scene, const tunable_parameters *tp)
 {
-    if (h->tp_valid && std::memcmp(&h->last_tp, tp, sizeof(*tp)) == 0) return SPH_OK;
+    if (h->tp_valid[scene] && std::memcmp(&h->last_tp[scene], tp, sizeof(*tp)) == 0) return SPH_OK;
     const int s = h->params_next;
     h->params_next = (s + 1) % h->params_ring;
     SPH_CUDA(cudaEventSynchronize(h->params_ev[s]));
     h->h_params_ring[s] = *tp;
-    SPH_CUDA(cudaMemcpyAsync(h->d_params, &h->h_params_ring[s], sizeof(*tp),
+    SPH_CUDA(cudaMemcpyAsync(&h->d_scenes[scene].P, &h->h_params_ring[s], sizeof(*tp),
                              cudaMemcpyHostToDevice, h->stream));
     SPH_CUDA(cudaEventRecord(h->params_ev[s], h->stream));
-    h->last_tp = *tp;
-    h->tp_valid = true;
+    h->last_tp[scene] = *tp;
+    h->tp_valid[scene] = 1;
+    h->scenes[scene].P = *tp;
     return SPH_OK;
 }
 
@@ -143,6 +146,15 @@ static int validate_tp(const tunable_parameters *tp)
     return SPH_OK;
 }
 
+static int validate_grid(float spacing, unsigned sx, unsigned sy)
+{
+    if (!(spacing > 0.0f) || sx == 0 || sy == 0 || (unsigned long long)sx * sy >= (1ull << 30)) {
+        set_error("invalid neighbour grid (spacing %g, %u x %u)", (double)spacing, sx, sy);
+        return SPH_ERR_INVALID;
+    }
+    return SPH_OK;
+}
+
 static int check_handle(sph_cuda *h)
 {
     if (!h) {
@@ -158,6 +170,155 @@ static int check_n(sph_cuda *h, int n)
         set_error("particle count %d outside [0, %d]", n, h->capacity);
         return n < 0 ? SPH_ERR_INVALID : SPH_ERR_CAPACITY;
     }
+    if (h->nscenes > 1 && n != h->capacity) {
+        set_error("an ensemble of %d scenes holds exactly %d particles (got %d)", h->nscenes,
+                  h->capacity, n);
+        return SPH_ERR_INVALID;
+    }
+    return SPH_OK;
+}
+
+static void free_all(sph_cuda *h)
+{
+    destroy_graph(h);
+    void *ptrs[] = {h->pos_a, h->vel_a, h->id_a, h->pos_b, h->prev_b, h->vel_b, h->kr_b,
+                    h->pos_c, h->prev_c, h->xr_c, h->mask01_c, h->mask2_c, h->id_c,
+                    h->tmp_id, h->cnt, h->start_a, h->start_c, h->tile_sums, h->d_scenes,
+                    h->d_p_off, h->d_nocell, h->d_state, h->d_partials, h->d_scratch};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    if (h->h_stage) cudaFreeHost(h->h_stage);
+    if (h->h_params_ring) cudaFreeHost(h->h_params_ring);
+    if (h->params_ev) {
+        for (int i = 0; i < h->params_ring; ++i)
+            if (h->params_ev[i]) cudaEventDestroy(h->params_ev[i]);
+        delete[] h->params_ev;
+    }
+    for (cudaEvent_t e : h->timer)
+        if (e) cudaEventDestroy(e);
+    if (h->own_stream) cudaStreamDestroy(h->own_stream);
+}
+
+// Uploads the scene table and the slot offsets (scene particle counts may
+// change between uploads of a single-scene handle).
+static int push_scenes(sph_cuda *h)
+{
+    std::vector<int> off(h->nscenes + 1);
+    int p = 0;
+    for (int s = 0; s < h->nscenes; ++s) {
+        h->scenes[s].p_off = p;
+        off[s] = p;
+        p += h->scenes[s].n;
+    }
+    off[h->nscenes] = p;
+    SPH_CUDA(cudaMemcpyAsync(h->d_scenes, h->scenes.data(), h->nscenes * sizeof(Scene),
+                             cudaMemcpyHostToDevice, h->stream));
+    SPH_CUDA(cudaMemcpyAsync(h->d_p_off, off.data(), (h->nscenes + 1) * sizeof(int),
+                             cudaMemcpyHostToDevice, h->stream));
+    SPH_CUDA(cudaStreamSynchronize(h->stream));  // host vectors go out of scope
+    for (int s = 0; s < h->nscenes; ++s) {
+        h->last_tp[s] = h->scenes[s].P;
+        h->tp_valid[s] = 1;
+    }
+    return SPH_OK;
+}
+
+// Allocates a handle for `scenes` (cell offsets filled in here).
+static int build_handle(sph_cuda **out, std::vector<Scene> &&scenes, int capacity, int max_bucket,
+                        int max_neighbors)
+{
+    *out = nullptr;
+    sph_cuda *h = new (std::nothrow) sph_cuda();
+    if (!h) {
+        set_error("host allocation failed");
+        return SPH_ERR_ALLOC;
+    }
+    auto fail = [&](int rc) {
+        free_all(h);
+        delete h;
+        return rc;
+    };
+    h->scenes = std::move(scenes);
+    h->nscenes = (int)h->scenes.size();
+    h->capacity = capacity;
+    h->max_bucket = max_bucket;
+    h->max_neighbors = max_neighbors;
+    h->last_tp.resize(h->nscenes);
+    h->tp_valid.assign(h->nscenes, 0);
+    long long m = 0;
+    for (Scene &s : h->scenes) {
+        s.c_off = (int)m;
+        s.max_bucket = max_bucket;
+        s.max_neighbors = max_neighbors;
+        m += (long long)s.ncells + 1;
+    }
+    if (m >= (1ll << 30)) {
+        set_error("%lld grid cells in total: above 2^30", m);
+        return fail(SPH_ERR_INVALID);
+    }
+    h->M = (int)m;
+    int dev = 0;
+    int rc = cuda_fail(cudaGetDevice(&dev), "cudaGetDevice");
+    if (!rc) rc = cuda_fail(cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, dev),
+                            "cudaDeviceGetAttribute");
+    if (rc) return fail(rc);
+    rc = cuda_fail(cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking),
+                   "cudaStreamCreate");
+    if (rc) return fail(rc);
+    h->stream = h->own_stream;
+    const size_t N = (size_t)capacity;
+    const size_t M = (size_t)h->M;
+    const size_t scan_items = std::max(M, N) + 1;
+    h->ntiles = (int)((scan_items + kScanTile - 1) / kScanTile);
+    h->npartials = 148 * 2;
+    const size_t nwords = (M + 31) / 32 + 1;
+    if ((rc = dalloc(&h->pos_a, N)) || (rc = dalloc(&h->vel_a, N)) || (rc = dalloc(&h->id_a, N)) ||
+        (rc = dalloc(&h->pos_b, N)) || (rc = dalloc(&h->prev_b, N)) ||
+        (rc = dalloc(&h->vel_b, N)) || (rc = dalloc(&h->kr_b, N)) || (rc = dalloc(&h->pos_c, N)) ||
+        (rc = dalloc(&h->prev_c, N)) || (rc = dalloc(&h->xr_c, N)) ||
+        (rc = dalloc(&h->mask01_c, N)) || (rc = dalloc(&h->mask2_c, N)) ||
+        (rc = dalloc(&h->id_c, N)) || (rc = dalloc(&h->tmp_id, N)) ||
+        (rc = dalloc(&h->cnt, std::max(M, N + 1))) ||
+        (rc = dalloc(&h->start_a, std::max(M + 1, N + 1))) || (rc = dalloc(&h->start_c, M + 1)) ||
+        (rc = dalloc(&h->tile_sums, (size_t)h->ntiles)) ||
+        (rc = dalloc(&h->d_scenes, (size_t)h->nscenes)) ||
+        (rc = dalloc(&h->d_p_off, (size_t)h->nscenes + 1)) || (rc = dalloc(&h->d_nocell, nwords)) ||
+        (rc = dalloc(&h->d_state, 1)) || (rc = dalloc(&h->d_partials, (size_t)h->npartials * 3 + 3)))
+        return fail(rc);
+    rc = cuda_fail(cudaMemsetAsync(h->cnt, 0, std::max(M, N + 1) * sizeof(unsigned), h->stream),
+                   "cudaMemset");
+    if (!rc) rc = cuda_fail(cudaMemsetAsync(h->d_state, 0, sizeof(DevState), h->stream), "cudaMemset");
+    if (rc) return fail(rc);
+    {
+        std::vector<unsigned> bits(nwords, 0u);
+        for (const Scene &s : h->scenes) {
+            const size_t k = (size_t)s.c_off + s.ncells;
+            bits[k >> 5] |= 1u << (k & 31);
+        }
+        rc = cuda_fail(cudaMemcpy(h->d_nocell, bits.data(), nwords * sizeof(unsigned),
+                                  cudaMemcpyHostToDevice),
+                       "no-cell bitmap");
+        if (rc) return fail(rc);
+    }
+    h->params_ring = 64;
+    rc = cuda_fail(cudaHostAlloc((void **)&h->h_params_ring,
+                                 h->params_ring * sizeof(tunable_parameters), cudaHostAllocDefault),
+                   "cudaHostAlloc");
+    if (rc) return fail(rc);
+    h->params_ev = new (std::nothrow) cudaEvent_t[h->params_ring]();
+    if (!h->params_ev) return fail(SPH_ERR_ALLOC);
+    for (int i = 0; i < h->params_ring; ++i) {
+        rc = cuda_fail(cudaEventCreateWithFlags(&h->params_ev[i], cudaEventDisableTiming),
+                       "cudaEventCreate");
+        if (rc) return fail(rc);
+    }
+    for (cudaEvent_t &e : h->timer) {
+        rc = cuda_fail(cudaEventCreate(&e), "cudaEventCreate");
+        if (rc) return fail(rc);
+    }
+    rc = push_scenes(h);
+    if (rc) return fail(rc);
+    *out = h;
     return SPH_OK;
 }
 
@@ -179,6 +340,10 @@ static int upload_common(sph_cuda *h, int n, Fill fill)
         prev[i] = make_float2(r[4], r[5]);
         xr[i] = make_float4(r[0], r[1], r[6], r[7]);
     }
+    if (h->nscenes == 1 && h->scenes[0].n != n) {
+        h->scenes[0].n = n;
+        SPH_TRY(push_scenes(h));
+    }
     h->n = n;
     const size_t b = (size_t)n * sizeof(float2);
     if (n > 0) {
@@ -197,7 +362,6 @@ static int upload_common(sph_cuda *h, int n, Fill fill)
 // pos, vel, prev, rho, pressure).  Synchronous.
 static int download_common(sph_cuda *h, int n, float2 **host)
 {
-    SPH_TRY(check_n(h, n));
     if (n != h->n) {
         set_error("download of %d particles, handle holds %d", n, h->n);
         return SPH_ERR_INVALID;
@@ -213,26 +377,17 @@ static int download_common(sph_cuda *h, int n, float2 **host)
     return SPH_OK;
 }
 
-static void free_all(sph_cuda *h)
+// The tunables a single-scene call passes (NULL = keep the current ones);
+// ensembles take their per-scene tunables from sph_cuda_set_scene_params.
+static int apply_tp(sph_cuda *h, const tunable_parameters *tp)
 {
-    destroy_graph(h);
-    void *ptrs[] = {h->pos_a, h->vel_a, h->id_a, h->pos_b, h->prev_b, h->vel_b, h->kr_b,
-                    h->pos_c, h->prev_c, h->xr_c, h->mask01_c, h->mask2_c, h->id_c,
-                    h->tmp_id, h->cnt, h->start_a,
-                    h->start_c, h->tile_sums, h->d_params, h->d_state, h->d_partials,
-                    h->d_scratch};
-    for (void *p : ptrs)
-        if (p) cudaFree(p);
-    if (h->h_stage) cudaFreeHost(h->h_stage);
-    if (h->h_params_ring) cudaFreeHost(h->h_params_ring);
-    if (h->params_ev) {
-        for (int i = 0; i < h->params_ring; ++i)
-            if (h->params_ev[i]) cudaEventDestroy(h->params_ev[i]);
-        delete[] h->params_ev;
+    if (!tp) return SPH_OK;
+    if (h->nscenes != 1) {
+        set_error("an ensemble takes per-scene tunables (sph_cuda_set_scene_params); pass NULL");
+        return SPH_ERR_INVALID;
     }
-    for (cudaEvent_t e : h->timer)
-        if (e) cudaEventDestroy(e);
-    if (h->own_stream) cudaStreamDestroy(h->own_stream);
+    SPH_TRY(validate_tp(tp));
+    return set_scene_params(h, 0, tp);
 }
 
 }  // namespace sph
@@ -255,12 +410,7 @@ int sph_cuda_create(sph_cuda_t **out, const param *params, const AABB_t *boundar
         set_error("max_particles %d < 0", max_particles);
         return SPH_ERR_INVALID;
     }
-    if (!(grid->spacing > 0.0f) || grid->size_x == 0 || grid->size_y == 0 ||
-        (unsigned long long)grid->size_x * grid->size_y >= (1ull << 30)) {
-        set_error("invalid neighbour grid (spacing %g, %u x %u)", (double)grid->spacing,
-                  grid->size_x, grid->size_y);
-        return SPH_ERR_INVALID;
-    }
+    SPH_TRY(validate_grid(grid->spacing, grid->size_x, grid->size_y));
     if (grid->max_bucket_size == 0 || grid->max_neighbors == 0) {
         set_error("max_bucket_size and max_neighbors must be positive");
         return SPH_ERR_INVALID;
@@ -271,78 +421,77 @@ int sph_cuda_create(sph_cuda_t **out, const param *params, const AABB_t *boundar
         return SPH_ERR_UNSUPPORTED;
     }
     SPH_TRY(validate_tp(&params->tunable_params));
-    sph_cuda *h = new (std::nothrow) sph_cuda();
-    if (!h) {
-        set_error("host allocation failed");
-        return SPH_ERR_ALLOC;
-    }
-    Grid &g = h->g;
-    g.spacing = grid->spacing;
-    g.size_x = (int)grid->size_x;
-    g.size_y = (int)grid->size_y;
-    g.ncells = g.size_x * g.size_y;
-    g.min_x = boundary->min_x;
-    g.max_x = boundary->max_x;
-    g.min_y = boundary->min_y;
-    g.max_y = boundary->max_y;
-    g.max_bucket = (int)grid->max_bucket_size;
-    g.max_neighbors = (int)grid->max_neighbors;
-    h->capacity = max_particles;
-
-    auto fail = [&](int rc) {
-        free_all(h);
-        delete h;
-        return rc;
-    };
-    int rc = cuda_fail(cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking),
-                       "cudaStreamCreate");
-    if (rc) return fail(rc);
-    h->stream = h->own_stream;
-    const size_t N = (size_t)max_particles;
-    const size_t C = (size_t)g.ncells;
-    const int scan_items = (int)((C + 1 > N ? C + 1 : N) + 1);
-    h->ntiles = (scan_items + kScanTile - 1) / kScanTile;
-    h->npartials = 148 * 2;
-    if ((rc = dalloc(&h->pos_a, N)) || (rc = dalloc(&h->vel_a, N)) || (rc = dalloc(&h->id_a, N)) ||
-        (rc = dalloc(&h->pos_b, N)) || (rc = dalloc(&h->prev_b, N)) ||
-        (rc = dalloc(&h->vel_b, N)) || (rc = dalloc(&h->kr_b, N)) || (rc = dalloc(&h->pos_c, N)) ||
-        (rc = dalloc(&h->prev_c, N)) || (rc = dalloc(&h->xr_c, N)) ||
-        (rc = dalloc(&h->mask01_c, N)) || (rc = dalloc(&h->mask2_c, N)) || (rc = dalloc(&h->id_c, N)) ||
-        (rc = dalloc(&h->tmp_id, N)) || (rc = dalloc(&h->cnt, C + 1 > N + 1 ? C + 1 : N + 1)) ||
-        (rc = dalloc(&h->start_a, C + 2 > N + 1 ? C + 2 : N + 1)) ||
-        (rc = dalloc(&h->start_c, C + 2)) || (rc = dalloc(&h->tile_sums, (size_t)h->ntiles)) ||
-        (rc = dalloc(&h->d_params, 1)) || (rc = dalloc(&h->d_state, 1)) ||
-        (rc = dalloc(&h->d_partials, (size_t)h->npartials * 3 + 3)))
-        return fail(rc);
-    rc = cuda_fail(cudaMemsetAsync(h->cnt, 0, (C + 1 > N + 1 ? C + 1 : N + 1) * sizeof(unsigned),
-                                   h->stream),
-                   "cudaMemset");
-    if (rc) return fail(rc);
-    rc = cuda_fail(cudaMemsetAsync(h->d_state, 0, sizeof(DevState), h->stream), "cudaMemset");
-    if (rc) return fail(rc);
-    h->params_ring = 64;
-    rc = cuda_fail(cudaHostAlloc((void **)&h->h_params_ring,
-                                 h->params_ring * sizeof(tunable_parameters), cudaHostAllocDefault),
-                   "cudaHostAlloc");
-    if (rc) return fail(rc);
-    h->params_ev = new (std::nothrow) cudaEvent_t[h->params_ring]();
-    if (!h->params_ev) return fail(SPH_ERR_ALLOC);
-    for (int i = 0; i < h->params_ring; ++i) {
-        rc = cuda_fail(cudaEventCreateWithFlags(&h->params_ev[i], cudaEventDisableTiming),
-                       "cudaEventCreate");
-        if (rc) return fail(rc);
-    }
-    for (cudaEvent_t &e : h->timer) {
-        rc = cuda_fail(cudaEventCreate(&e), "cudaEventCreate");
-        if (rc) return fail(rc);
-    }
-    rc = set_params(h, &params->tunable_params);
-    if (rc) return fail(rc);
-    rc = cuda_fail(cudaStreamSynchronize(h->stream), "create sync");
-    if (rc) return fail(rc);
-    *out = h;
-    return SPH_OK;
+    Scene s{};
+    s.P = params->tunable_params;
+    s.spacing = grid->spacing;
+    s.size_x = (int)grid->size_x;
+    s.size_y = (int)grid->size_y;
+    s.ncells = s.size_x * s.size_y;
+    s.n = 0;
+    s.min_x = boundary->min_x;
+    s.max_x = boundary->max_x;
+    s.min_y = boundary->min_y;
+    s.max_y = boundary->max_y;
+    std::vector<Scene> v(1, s);
+    return build_handle(out, std::move(v), max_particles, (int)grid->max_bucket_size,
+                        (int)grid->max_neighbors);
 }
+
+int sph_cuda_create_ensemble(sph_cuda_t **out, const sph_scene_desc *descs, int nscenes,
+                             int max_bucket, int max_neighbors)
+{
+    if (!out || !descs || nscenes <= 0) {
+        set_error("sph_cuda_create_ensemble: null argument or no scenes");
+        return SPH_ERR_INVALID;
+    }
+    *out = nullptr;
+    if (max_bucket <= 0 || max_neighbors <= 0) {
+        set_error("max_bucket and max_neighbors must be positive");
+        return SPH_ERR_INVALID;
+    }
+    std::vector<Scene> v((size_t)nscenes);
+    long long total = 0;
+    for (int i = 0; i < nscenes; ++i) {
+        const sph_scene_desc &d = descs[i];
+        SPH_TRY(validate_grid(d.spacing, d.size_x, d.size_y));
+        SPH_TRY(validate_tp(&d.params));
+        if (d.n < 0) {
+            set_error("scene %d has %d particles", i, d.n);
+            return SPH_ERR_INVALID;
+        }
+        Scene &s = v[i];
+        s = Scene{};
+        s.P = d.params;
+        s.spacing = d.spacing;
+        s.size_x = (int)d.size_x;
+        s.size_y = (int)d.size_y;
+        s.ncells = s.size_x * s.size_y;
+        s.n = d.n;
+        s.min_x = d.boundary.min_x;
+        s.max_x = d.boundary.max_x;
+        s.min_y = d.boundary.min_y;
+        s.max_y = d.boundary.max_y;
+        total += d.n;
+    }
+    if (total >= (1ll << 31)) {
+        set_error("%lld particles in total: above 2^31", total);
+        return SPH_ERR_INVALID;
+    }
+    return build_handle(out, std::move(v), (int)total, max_bucket, max_neighbors);
+}
+
+int sph_cuda_set_scene_params(sph_cuda_t *h, int scene, const tunable_parameters *tp)
+{
+    SPH_TRY(check_handle(h));
+    if (scene < 0 || scene >= h->nscenes) {
+        set_error("scene %d outside [0, %d)", scene, h->nscenes);
+        return SPH_ERR_INVALID;
+    }
+    SPH_TRY(validate_tp(tp));
+    return set_scene_params(h, scene, tp);
+}
+
+int sph_cuda_num_scenes(sph_cuda_t *h) { return h ? h->nscenes : 0; }
 
 int sph_cuda_destroy(sph_cuda_t *h)
 {
@@ -412,12 +561,11 @@ int sph_cuda_upload_soa(sph_cuda_t *h, const float *x, const float *y, const flo
 int sph_cuda_step(sph_cuda_t *h, const tunable_parameters *tp, int nsteps)
 {
     SPH_TRY(check_handle(h));
-    SPH_TRY(validate_tp(tp));
     if (nsteps < 0) {
         set_error("nsteps %d < 0", nsteps);
         return SPH_ERR_INVALID;
     }
-    SPH_TRY(set_params(h, tp));
+    SPH_TRY(apply_tp(h, tp));
     return run_steps(h, nsteps);
 }
 
@@ -429,8 +577,7 @@ int sph_cuda_step_schedule(sph_cuda_t *h, const tunable_parameters *tps, int nst
         return SPH_ERR_INVALID;
     }
     for (int t = 0; t < nsteps; ++t) {
-        SPH_TRY(validate_tp(&tps[t]));
-        SPH_TRY(set_params(h, &tps[t]));
+        SPH_TRY(apply_tp(h, &tps[t]));
         SPH_TRY(run_steps(h, 1));
     }
     return SPH_OK;
@@ -564,6 +711,25 @@ int sph_cuda_diagnostics(sph_cuda_t *h, double out[3])
     return SPH_OK;
 }
 
+int sph_cuda_scene_diagnostics(sph_cuda_t *h, double *out)
+{
+    SPH_TRY(check_handle(h));
+    if (!out) {
+        set_error("null output");
+        return SPH_ERR_INVALID;
+    }
+    if (h->n == 0) {
+        for (int s = 0; s < 3 * h->nscenes; ++s) out[s] = 0.0;
+        return SPH_OK;
+    }
+    const size_t b = (size_t)h->nscenes * 3 * sizeof(double);
+    SPH_TRY(ensure_scratch(h, b + 16));
+    SPH_TRY(launch_scene_diagnostics(h, (double *)h->d_scratch));
+    SPH_CUDA(cudaMemcpyAsync(out, h->d_scratch, b, cudaMemcpyDeviceToHost, h->stream));
+    SPH_CUDA(cudaStreamSynchronize(h->stream));
+    return SPH_OK;
+}
+
 int sph_cuda_neighbor_lists(sph_cuda_t *h, int *counts, int *ids, long long max_total,
                             long long *total)
 {
@@ -593,7 +759,6 @@ int sph_cuda_neighbor_lists(sph_cuda_t *h, int *counts, int *ids, long long max_
         return SPH_ERR_CAPACITY;
     }
     if (tot == 0) return SPH_OK;
-    // Counts were read before the scan zeroed nothing (zero_input = false).
     int *d_ids = nullptr;
     SPH_CUDA(cudaMallocAsync((void **)&d_ids, (size_t)tot * sizeof(int), h->stream));
     int rc = launch_half_lists(h, nullptr, d_off, d_ids, true);
@@ -609,7 +774,11 @@ int sph_cuda_neighbor_lists(sph_cuda_t *h, int *counts, int *ids, long long max_
 static int probe(sph_cuda *h, const tunable_parameters *tp, int which, float *a, float *b)
 {
     SPH_TRY(check_handle(h));
-    SPH_TRY(validate_tp(tp));
+    if (tp) SPH_TRY(validate_tp(tp));
+    if (tp && h->nscenes != 1) {
+        set_error("probes of an ensemble use each scene's own tunables; pass NULL");
+        return SPH_ERR_INVALID;
+    }
     const int n = h->n;
     if (n == 0) return SPH_OK;
     if (!a || !b) {
@@ -621,13 +790,12 @@ static int probe(sph_cuda *h, const tunable_parameters *tp, int which, float *a,
     SPH_TRY(ensure_stage(h, (size_t)n * sizeof(float2) + 16));
     float2 *out = (float2 *)((char *)h->d_scratch + sb);
     // probes use their own parameters without disturbing the step's
-    const tunable_parameters saved = h->last_tp;
-    const bool had = h->tp_valid;
-    SPH_TRY(set_params(h, tp));
+    const tunable_parameters saved = h->scenes[0].P;
+    if (tp) SPH_TRY(set_scene_params(h, 0, tp));
     SPH_TRY(launch_probe(h, which, h->d_scratch, out));
     SPH_CUDA(cudaMemcpyAsync(h->h_stage, out, (size_t)n * sizeof(float2), cudaMemcpyDeviceToHost,
                              h->stream));
-    if (had) SPH_TRY(set_params(h, &saved));
+    if (tp) SPH_TRY(set_scene_params(h, 0, &saved));
     SPH_CUDA(cudaStreamSynchronize(h->stream));
     const float2 *s = (const float2 *)h->h_stage;
     for (int i = 0; i < n; ++i) {
@@ -656,14 +824,13 @@ int sph_cuda_kernel_times(sph_cuda_t *h, const tunable_parameters *tp, float *ms
                           int *count)
 {
     SPH_TRY(check_handle(h));
-    SPH_TRY(validate_tp(tp));
     if (!ms || !count) {
         set_error("null output");
         return SPH_ERR_INVALID;
     }
     *count = 0;
+    SPH_TRY(apply_tp(h, tp));
     if (h->n == 0) return SPH_OK;
-    SPH_TRY(set_params(h, tp));
     cudaEvent_t ev[kMaxKernelsPerStep + 1];
     const int ne = step_kernel_count() + 1;
     for (int i = 0; i < ne; ++i) SPH_CUDA(cudaEventCreate(&ev[i]));
@@ -684,6 +851,93 @@ int sph_cuda_launches_per_step(sph_cuda_t *h)
 {
     if (!h) return 0;
     return step_kernel_count();
+}
+
+int sph_cuda_set_launch_shapes(sph_cuda_t *h, const int *shapes)
+{
+    SPH_TRY(check_handle(h));
+    if (!shapes) {
+        set_error("null shapes");
+        return SPH_ERR_INVALID;
+    }
+    for (int k = 0; k < kGathers; ++k) {
+        const int b = shapes[2 * k], p = shapes[2 * k + 1];
+        const int max_b = k == 2 ? kBlock : kMaxBlock;  // relax_update is built for <= 256
+        if (b < 32 || b > max_b || (b & 31) || p < 0 || p > 32) {
+            set_error("launch shape %d: block %d (32..%d, multiple of 32), persistent %d (0..32)",
+                      k, b, max_b, p);
+            return SPH_ERR_INVALID;
+        }
+    }
+    for (int k = 0; k < kGathers; ++k) {
+        h->shape[k].block = shapes[2 * k];
+        h->shape[k].persistent = shapes[2 * k + 1];
+    }
+    destroy_graph(h);
+    return SPH_OK;
+}
+
+int sph_cuda_get_launch_shapes(sph_cuda_t *h, int *shapes)
+{
+    SPH_TRY(check_handle(h));
+    if (!shapes) {
+        set_error("null shapes");
+        return SPH_ERR_INVALID;
+    }
+    for (int k = 0; k < kGathers; ++k) {
+        shapes[2 * k] = h->shape[k].block;
+        shapes[2 * k + 1] = h->shape[k].persistent;
+    }
+    return SPH_OK;
+}
+
+// Tries each candidate launch shape on the three gathers for `trial_steps`
+// steps (which advance the simulation) and keeps, per gather, the shape with
+// the lowest median CUDA-event time.
+int sph_cuda_autotune(sph_cuda_t *h, int trial_steps, int *shapes_out)
+{
+    SPH_TRY(check_handle(h));
+    if (trial_steps <= 0) trial_steps = 3;
+    if (h->n == 0) {
+        if (shapes_out) SPH_TRY(sph_cuda_get_launch_shapes(h, shapes_out));
+        return SPH_OK;
+    }
+    static const Shape cands[] = {{128, 0}, {256, 0}, {512, 0}, {256, 2}, {256, 4},
+                                  {128, 8}, {512, 1}, {512, 2}};
+    const int nc = (int)(sizeof(cands) / sizeof(cands[0]));
+    float best[kGathers];
+    Shape pick[kGathers];
+    for (int k = 0; k < kGathers; ++k) {
+        best[k] = 3.4e38f;
+        pick[k] = h->shape[k];
+    }
+    const int gather_idx[kGathers] = {0, 5, 6};  // positions in the step's kernel order
+    for (int c = 0; c < nc; ++c) {
+        for (int k = 0; k < kGathers; ++k) {
+            Shape s = cands[c];
+            if (k == 2 && s.block > kBlock) s.block = kBlock;
+            h->shape[k] = s;
+        }
+        std::vector<float> t[kGathers];
+        for (int r = 0; r < trial_steps; ++r) {
+            float ms[kMaxKernelsPerStep];
+            int cnt = 0;
+            SPH_TRY(sph_cuda_kernel_times(h, nullptr, ms, kMaxKernelsPerStep, &cnt));
+            for (int k = 0; k < kGathers; ++k) t[k].push_back(ms[gather_idx[k]]);
+        }
+        for (int k = 0; k < kGathers; ++k) {
+            std::sort(t[k].begin(), t[k].end());
+            const float med = t[k][t[k].size() / 2];
+            if (med < best[k]) {
+                best[k] = med;
+                pick[k] = h->shape[k];
+            }
+        }
+    }
+    for (int k = 0; k < kGathers; ++k) h->shape[k] = pick[k];
+    destroy_graph(h);
+    if (shapes_out) SPH_TRY(sph_cuda_get_launch_shapes(h, shapes_out));
+    return SPH_OK;
 }
 
 int sph_cuda_timer_start(sph_cuda_t *h)

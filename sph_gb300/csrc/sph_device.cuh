@@ -5,19 +5,67 @@
 
 namespace sph {
 
-// hash_val (hash.c:35-47): key = floor(y/s) * size_x + floor(x/s), with the
-// IEEE float division of the reference.  x == size_x * s aliases cell
-// (0, gy+1) exactly as in the reference.  Keys outside [0, ncells) -- a
-// negative or NaN coordinate, or y == size_y * s -- are undefined behaviour
-// there; here they map to the "no cell" bucket `ncells`.
-__device__ __forceinline__ unsigned cell_key(float x, float y, const Grid &g)
+// The scene of a particle slot (slots of a scene are contiguous, and ids
+// follow the same ranges): the last s with p_off[s] <= i.
+__device__ __forceinline__ int scene_of(const Ctx &c, int i)
+{
+    if (c.nscenes == 1) return 0;
+    int lo = 0, hi = c.nscenes;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(c.p_off + mid) <= i) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// A scene's grid, as the cell keys and stencils use it.
+struct SG {
+    float spacing;
+    int size_x, size_y, ncells, c_off;
+};
+
+__device__ __forceinline__ SG load_grid(const Scene *__restrict__ S)
+{
+    SG g;
+    g.spacing = __ldg(&S->spacing);
+    g.size_x = __ldg(&S->size_x);
+    g.size_y = __ldg(&S->size_y);
+    g.ncells = __ldg(&S->ncells);
+    g.c_off = __ldg(&S->c_off);
+    return g;
+}
+
+// A scene's box: min_x, max_x, min_y, max_y.
+__device__ __forceinline__ float4 load_box(const Scene *__restrict__ S)
+{
+    return make_float4(__ldg(&S->min_x), __ldg(&S->max_x), __ldg(&S->min_y), __ldg(&S->max_y));
+}
+
+__device__ __forceinline__ tunable_parameters load_params(const Scene *__restrict__ S)
+{
+    tunable_parameters P;
+    const float4 *src = reinterpret_cast<const float4 *>(&S->P);
+    float4 *dst = reinterpret_cast<float4 *>(&P);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) dst[k] = __ldg(src + k);
+    return P;
+}
+
+// hash_val (hash.c:35-47): local key = floor(y/s) * size_x + floor(x/s), with
+// the IEEE float division of the reference, returned as a global key
+// (c_off + local).  x == size_x * s aliases cell (0, gy+1) exactly as in the
+// reference.  Keys outside [0, ncells) -- a negative or NaN coordinate, or
+// y == size_y * s -- are undefined behaviour there; here they map to the
+// scene's "no cell" bucket c_off + ncells.
+__device__ __forceinline__ unsigned cell_key(float x, float y, const SG &g)
 {
     const float fx = floorf(__fdiv_rn(x, g.spacing));
     const float fy = floorf(__fdiv_rn(y, g.spacing));
     if (!(fx >= 0.0f) || !(fy >= 0.0f) || fx > 1073741824.0f || fy > 1073741824.0f)
-        return (unsigned)g.ncells;
+        return (unsigned)(g.c_off + g.ncells);
     const long long k = (long long)(unsigned)fy * g.size_x + (long long)(unsigned)fx;
-    return k < g.ncells ? (unsigned)k : (unsigned)g.ncells;
+    return (unsigned)(g.c_off + (k < g.ncells ? (int)k : g.ncells));
 }
 
 // checkVelocity, fluid.c:613-625
@@ -29,7 +77,7 @@ __device__ __forceinline__ float clamp5(float v)
 // boundaryConditions, fluid.c:656-744.  Rounded step by step (no fused
 // multiply-add) so the per-particle arithmetic equals the reference's.
 __device__ __forceinline__ void boundary(float &x, float &y, const tunable_parameters &P,
-                                         const Grid &g)
+                                         const float4 &box)
 {
     const float cx = P.mover_center_x, cy = P.mover_center_y;
     if (P.mover_type == SPHERE_MOVER) {
@@ -58,10 +106,23 @@ __device__ __forceinline__ void boundary(float &x, float &y, const tunable_param
             }
         }
     }
-    if (x < g.min_x) x = g.min_x;
-    else if (x > g.max_x) x = __fsub_rn(g.max_x, 0.001f);
-    if (y < g.min_y) y = g.min_y;
-    else if (y > g.max_y) y = __fsub_rn(g.max_y, 0.001f);
+    if (x < box.x) x = box.x;
+    else if (x > box.y) x = __fsub_rn(box.y, 0.001f);
+    if (y < box.z) y = box.z;
+    else if (y > box.w) y = __fsub_rn(box.w, 0.001f);
+}
+
+// boundaryConditions with the scene's mover and box, read at the call (kept
+// out of the registers of the gather loops that precede it).
+__device__ __forceinline__ void boundary_of(float &x, float &y, const Scene *__restrict__ S)
+{
+    tunable_parameters P;
+    P.mover_center_x = __ldg(&S->P.mover_center_x);
+    P.mover_center_y = __ldg(&S->P.mover_center_y);
+    P.mover_width = __ldg(&S->P.mover_width);
+    P.mover_height = __ldg(&S->P.mover_height);
+    P.mover_type = (char)__ldg(reinterpret_cast<const signed char *>(&S->P.mover_type));
+    boundary(x, y, P, load_box(S));
 }
 
 // r^2 rounded exactly as the reference computes it (two products, one sum,
@@ -79,16 +140,18 @@ __device__ __forceinline__ float dist2(float dx, float dy)
 // only the first max_bucket_size particles of a bucket.
 template <class F>
 __device__ __forceinline__ void for_each_candidate(unsigned key, const int *__restrict__ start,
-                                                   const Grid &g, bool capped, F &&f)
+                                                   const SG &g, bool capped, int max_bucket,
+                                                   F &&f)
 {
-    const int gy = (int)(key / (unsigned)g.size_x);
-    const int gx = (int)key - gy * g.size_x;
+    const int lk = (int)key - g.c_off;
+    const int gy = lk / g.size_x;
+    const int gx = lk - gy * g.size_x;
     const int x0 = gx > 0 ? gx - 1 : 0;
     const int x1 = gx + 1 < g.size_x ? gx + 1 : g.size_x - 1;
     const int y0 = gy > 0 ? gy - 1 : 0;
     const int y1 = gy + 1 < g.size_y ? gy + 1 : g.size_y - 1;
     for (int y = y0; y <= y1; ++y) {
-        const int row = y * g.size_x;
+        const int row = g.c_off + y * g.size_x;
         if (!capped) {
             const int a = __ldg(start + row + x0), b = __ldg(start + row + x1 + 1);
             for (int j = a; j < b; ++j) f(j);
@@ -96,30 +159,32 @@ __device__ __forceinline__ void for_each_candidate(unsigned key, const int *__re
             for (int x = x0; x <= x1; ++x) {
                 const int a = __ldg(start + row + x);
                 const int e = __ldg(start + row + x + 1);
-                const int b = e - a > g.max_bucket ? a + g.max_bucket : e;
+                const int b = e - a > max_bucket ? a + max_bucket : e;
                 for (int j = a; j < b; ++j) f(j);
             }
         }
     }
 }
 
-// A particle takes part in the neighbour search if its key is in the grid
-// and, when some cell overflowed, it is among its cell's first max_bucket.
+// A particle takes part in the neighbour search if its key is in its
+// scene's grid and, when some cell overflowed, it is among its cell's first
+// max_bucket.
 __device__ __forceinline__ bool searchable(unsigned key, int slot, const int *__restrict__ start,
-                                           const Grid &g, bool capped)
+                                           const SG &g, bool capped, int max_bucket)
 {
-    if (key >= (unsigned)g.ncells) return false;
-    return !capped || slot - __ldg(start + key) < g.max_bucket;
+    if ((int)key - g.c_off >= g.ncells) return false;
+    return !capped || slot - __ldg(start + key) < max_bucket;
 }
 
 // The three stencil rows of a cell (slot 0: gy-1, 1: gy, 2: gy+1), each the
 // contiguous range [a[r], a[r] + len[r]) of sorted slots (empty outside the
 // grid).  Valid when no cell overflowed its bucket cap.
 __device__ __forceinline__ void stencil_rows(unsigned key, const int *__restrict__ start,
-                                             const Grid &g, int (&a)[3], int (&len)[3])
+                                             const SG &g, int (&a)[3], int (&len)[3])
 {
-    const int gy = (int)(key / (unsigned)g.size_x);
-    const int gx = (int)key - gy * g.size_x;
+    const int lk = (int)key - g.c_off;
+    const int gy = lk / g.size_x;
+    const int gx = lk - gy * g.size_x;
     const int x0 = gx > 0 ? gx - 1 : 0;
     const int x1 = gx + 1 < g.size_x ? gx + 1 : g.size_x - 1;
 #pragma unroll
@@ -129,7 +194,7 @@ __device__ __forceinline__ void stencil_rows(unsigned key, const int *__restrict
             a[r] = 0;
             len[r] = 0;
         } else {
-            const int row = y * g.size_x;
+            const int row = g.c_off + y * g.size_x;
             a[r] = __ldg(start + row + x0);
             len[r] = __ldg(start + row + x1 + 1) - a[r];
         }

@@ -4,20 +4,42 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 #include "sph_cuda.h"
 
 namespace sph {
 
-// Neighbour grid as the kernels see it.  Cell key = gy * size_x + gx
-// (hash.c:35-47); key `ncells` is the "no cell" bucket that collects
-// particles whose key falls outside the grid.
-struct Grid {
+// One scene -- an independent domain with its own box, grid and tunables --
+// as the kernels see it.  A handle holds one scene (the compute rank's
+// domain) or many (an ensemble).  Cell keys are global: a scene's local key
+// gy * size_x + gx (hash.c:35-47) is offset by c_off, and local key
+// `ncells` is the scene's own "no cell" bucket for particles whose key falls
+// outside its grid.  Sorting by global key keeps each scene's particles in
+// the contiguous slot range [p_off, p_off + n), in the id range of the same
+// bounds.
+struct Scene {
+    tunable_parameters P;  // first member: per-step updates copy into it
     float spacing;
     int size_x, size_y;
     int ncells;
+    int c_off;
+    int p_off;
+    int n;
     float min_x, max_x, min_y, max_y;
     int max_bucket;
     int max_neighbors;
+    int pad[3];
+};
+static_assert(sizeof(Scene) % 16 == 0, "Scene is loaded as an aligned record");
+
+// What every particle kernel receives by value.
+struct Ctx {
+    const Scene *scenes;
+    const int *p_off;  // nscenes + 1 slot offsets (p_off[s] = scenes[s].p_off)
+    int nscenes;
+    int n;             // particles of all scenes
+    int max_bucket;    // bucket cap, the same in every scene
 };
 
 // Device-resident counters and flags of one handle.
@@ -37,9 +59,19 @@ enum BuildSlot { SLOT_PREDICTED = 0, SLOT_RELAXED = 1, SLOT_UPLOAD = 2, SLOT_PRO
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = 16;                        // per thread
 constexpr int kScanTile = kScanThreads * kScanItems;  // cells per scan tile
-constexpr int kBlock = 256;                           // particle kernels
+constexpr int kBlock = 256;                           // default particle-kernel block
+constexpr int kMaxBlock = 512;                        // largest block an autotuner may pick
 constexpr int kRankScanMax = 1024;  // cells above this population use atomic order
 constexpr int kMaxKernelsPerStep = 16;
+constexpr int kGathers = 3;         // viscosity_predict, density, relax_update
+
+// Launch shape of one gather kernel: threads per block, and 0 for one block
+// per tile of particles or the number of resident blocks per SM for a
+// persistent grid-stride launch.
+struct Shape {
+    int block = kBlock;
+    int persistent = 0;
+};
 
 }  // namespace sph
 
@@ -48,11 +80,19 @@ constexpr int kMaxKernelsPerStep = 16;
 //   *_b : scratch in the order of the pass that wrote it
 //   *_c : sorted by (cell of the predicted position, id)
 struct sph_cuda {
-    sph::Grid g;
+    std::vector<sph::Scene> scenes;  // host copy of the scene table
+    int nscenes = 0;
+    int M = 0;                       // cell counters of all scenes (cells + no-cell buckets)
+    int max_bucket = 0, max_neighbors = 0;
     int capacity = 0;
     int n = 0;
+    int num_sms = 0;
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
+
+    sph::Scene *d_scenes = nullptr;
+    int *d_p_off = nullptr;
+    unsigned *d_nocell = nullptr;  // bit per cell counter: set for the no-cell buckets
 
     float2 *pos_a = nullptr, *vel_a = nullptr;
     int *id_a = nullptr;
@@ -64,13 +104,12 @@ struct sph_cuda {
     unsigned long long *mask2_c = nullptr;  // ... and row 2
     int *id_c = nullptr;
     int *tmp_id = nullptr;
-    unsigned int *cnt = nullptr;  // ncells + 1 counters, zero between builds
-    int *start_a = nullptr;       // ncells + 2 cell starts for the *_a order
-    int *start_c = nullptr;       // ncells + 2 cell starts for the *_c order
+    unsigned int *cnt = nullptr;  // M counters, zero between builds
+    int *start_a = nullptr;       // M + 1 cell starts for the *_a order
+    int *start_c = nullptr;       // M + 1 cell starts for the *_c order
     int *tile_sums = nullptr;
     int ntiles = 0;
 
-    tunable_parameters *d_params = nullptr;
     sph::DevState *d_state = nullptr;
     double *d_partials = nullptr;
     int npartials = 0;
@@ -86,8 +125,10 @@ struct sph_cuda {
     cudaEvent_t *params_ev = nullptr;
     int params_ring = 0;
     int params_next = 0;
-    tunable_parameters last_tp;
-    bool tp_valid = false;
+    std::vector<tunable_parameters> last_tp;  // per scene, as last copied
+    std::vector<char> tp_valid;
+
+    sph::Shape shape[sph::kGathers];  // launch shapes of the gathers (autotuned)
 
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -102,13 +143,23 @@ namespace sph {
 void set_error(const char *fmt, ...);
 int cuda_fail(cudaError_t e, const char *what);
 
+inline Ctx make_ctx(const sph_cuda *h)
+{
+    Ctx c;
+    c.scenes = h->d_scenes;
+    c.p_off = h->d_p_off;
+    c.nscenes = h->nscenes;
+    c.n = h->n;
+    c.max_bucket = h->max_bucket;
+    return c;
+}
+
 // Core operations shared by the fast API and the legacy entry points.
 int ensure_scratch(sph_cuda *h, size_t bytes);
 int ensure_stage(sph_cuda *h, size_t bytes);
 int upload_soa_device(sph_cuda *h, int n);  // pos_b/vel_b (id order) + xr_c -> state
-int set_params(sph_cuda *h, const tunable_parameters *tp);
+int set_scene_params(sph_cuda *h, int scene, const tunable_parameters *tp);
 int enqueue_step(sph_cuda *h, cudaEvent_t *events, int *nkernels);
 int run_steps(sph_cuda *h, int nsteps);
-int neighbor_lists(sph_cuda *h, int *counts, int *ids, long long max_total, long long *total);
 
 }  // namespace sph

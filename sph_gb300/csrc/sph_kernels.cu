@@ -11,6 +11,10 @@
 //   scan_reduce/apply   cell starts of the relaxed positions                     (A cells)
 //   scatter, permute    back into (cell, id) order                              (B -> A)
 //
+// A handle holds one scene or many (an ensemble): every kernel runs over the
+// particles of all scenes at once, each particle reading its own scene's
+// grid and tunables from the scene table.
+//
 // Every pass is a gather: a thread owns one particle (in sorted order) and
 // reads its 3x3 cell stencil, so no floating-point atomics exist and every
 // sum is taken in a fixed order: the results are deterministic.  The only
@@ -75,60 +79,61 @@ __device__ __forceinline__ unsigned block_exclusive_scan(unsigned v, unsigned *s
 // cell build: histogram scan, scatter, permute
 // ---------------------------------------------------------------------------
 
-// Per-tile sums of the histogram (and occupancy statistics of the cells).
+// Per-tile sums of the histogram, and occupancy statistics of the in-grid
+// cells (`nocell` has a bit set for every scene's no-cell bucket).
 __global__ void __launch_bounds__(kScanThreads)
-k_scan_reduce(const unsigned *__restrict__ in, int M, int ncells, int *__restrict__ tile_sums,
-              DevState *__restrict__ st, unsigned *occ, int max_bucket, int max_neighbors)
+k_scan_reduce(const unsigned *__restrict__ in, int M, const unsigned *__restrict__ nocell,
+              int *__restrict__ tile_sums, DevState *__restrict__ st, unsigned *occ,
+              int max_bucket, int max_neighbors)
 {
     __shared__ unsigned sh_s[kScanThreads / 32], sh_m[kScanThreads / 32];
-    __shared__ unsigned long long sh_e[kScanThreads / 32];
+    __shared__ unsigned long long sh_e[kScanThreads / 32], sh_o[kScanThreads / 32];
     const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
     unsigned s = 0, mx = 0;
-    unsigned long long excess = 0;
+    unsigned long long excess = 0, outside = 0;
+    unsigned v[kScanItems];
     if (base + kScanItems <= M) {
         const uint4 *p = reinterpret_cast<const uint4 *>(in + base);
 #pragma unroll
         for (int q = 0; q < kScanItems / 4; ++q) {
-            const uint4 v = p[q];
-            const unsigned w[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-                const int idx = base + 4 * q + e;
-                s += w[e];
-                if (idx < ncells) {
-                    mx = max(mx, w[e]);
-                    if (w[e] > (unsigned)max_bucket) excess += w[e] - max_bucket;
-                }
-            }
+            const uint4 t = p[q];
+            v[4 * q] = t.x; v[4 * q + 1] = t.y; v[4 * q + 2] = t.z; v[4 * q + 3] = t.w;
         }
     } else {
-        for (int e = 0; e < kScanItems; ++e) {
-            const int idx = base + e;
-            const unsigned v = idx < M ? in[idx] : 0u;
-            s += v;
-            if (idx < ncells) {
-                mx = max(mx, v);
-                if (v > (unsigned)max_bucket) excess += v - max_bucket;
-            }
+#pragma unroll
+        for (int e = 0; e < kScanItems; ++e) v[e] = base + e < M ? in[base + e] : 0u;
+    }
+    // the thread's 16 counters lie in one 32-bit word of the no-cell bitmap
+    const unsigned bits = (nocell && base < M) ? (__ldg(nocell + (base >> 5)) >> (base & 31)) : 0u;
+#pragma unroll
+    for (int e = 0; e < kScanItems; ++e) {
+        s += v[e];
+        if ((bits >> e) & 1u) {
+            outside += v[e];
+        } else {
+            mx = max(mx, v[e]);
+            if (v[e] > (unsigned)max_bucket) excess += v[e] - max_bucket;
         }
     }
-    if (occ && ncells < M && base <= ncells && ncells < base + kScanItems)
-        atomicAdd(&st->out_of_grid, (unsigned long long)in[ncells]);
     s = warp_sum(s);
     mx = warp_max(mx);
     excess = warp_sum(excess);
+    outside = warp_sum(outside);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) { sh_s[warp] = s; sh_m[warp] = mx; sh_e[warp] = excess; }
+    if (lane == 0) { sh_s[warp] = s; sh_m[warp] = mx; sh_e[warp] = excess; sh_o[warp] = outside; }
     __syncthreads();
     if (threadIdx.x == 0) {
         unsigned ts = 0, tm = 0;
-        unsigned long long te = 0;
-        for (int w = 0; w < kScanThreads / 32; ++w) { ts += sh_s[w]; tm = max(tm, sh_m[w]); te += sh_e[w]; }
+        unsigned long long te = 0, to = 0;
+        for (int w = 0; w < kScanThreads / 32; ++w) {
+            ts += sh_s[w]; tm = max(tm, sh_m[w]); te += sh_e[w]; to += sh_o[w];
+        }
         tile_sums[blockIdx.x] = (int)ts;
         if (occ) {
             atomicMax(occ, tm);
             atomicMax(&st->max_occ, tm);
             if (te) atomicAdd(&st->bucket_overflow, te);
+            if (to) atomicAdd(&st->out_of_grid, to);
             const unsigned m = tm < (unsigned)max_bucket ? tm : (unsigned)max_bucket;
             if (m > 0 && 5u * m - 1u > (unsigned)max_neighbors) atomicOr(&st->list_cap_risk, 1u);
         }
@@ -243,7 +248,7 @@ k_permute(int n, const uint2 *__restrict__ kr, const int *__restrict__ start,
         r = 0;
         for (int j = s0; j < s1; ++j) r += __ldg(tmp + j) < myid;
     } else {
-        r = (int)k.y;  // pathological cell: arrival order (see DESIGN.md)
+        r = (int)k.y;  // pathological cell: arrival order
     }
     const int d = s0 + r;
     id_dst[d] = myid;
@@ -251,14 +256,15 @@ k_permute(int n, const uint2 *__restrict__ kr, const int *__restrict__ start,
     if (b_src) b_dst[d] = b_src[i];
 }
 
-// Cell keys of uploaded positions (no step before them).
+// Cell keys of uploaded positions (id order, no step before them).
 __global__ void __launch_bounds__(kBlock)
-k_keys(int n, Grid g, const float2 *__restrict__ pos, uint2 *__restrict__ kr,
-       unsigned *__restrict__ cnt, unsigned *occ_reset)
+k_keys(Ctx c, const float2 *__restrict__ pos, uint2 *__restrict__ kr, unsigned *__restrict__ cnt,
+       unsigned *occ_reset)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0 && occ_reset) *occ_reset = 0u;
-    if (i >= n) return;
+    if (i >= c.n) return;
+    const SG g = load_grid(c.scenes + scene_of(c, i));
     const float2 p = pos[i];
     const unsigned key = cell_key(p.x, p.y, g);
     kr[i] = make_uint2(key, atomicAdd(cnt + key, 1u));
@@ -275,26 +281,20 @@ k_keys(int n, Grid g, const float2 *__restrict__ pos, uint2 *__restrict__ kr,
 // u = ((v_i - v_j).(x_j - x_i))/r, all from the velocities after gravity.
 // PROBE writes dv instead of advancing.
 template <bool PROBE>
-__global__ void __launch_bounds__(kBlock)
-k_viscosity_predict(int n, Grid g, const tunable_parameters *__restrict__ dP,
-                    DevState *__restrict__ st, const float2 *__restrict__ pos,
-                    const float2 *__restrict__ vel, const int *__restrict__ start,
-                    const unsigned *__restrict__ occ_in, unsigned *occ_reset,
-                    float2 *__restrict__ pos_out, float2 *__restrict__ prev_out,
-                    uint2 *__restrict__ kr_out, unsigned *__restrict__ cnt,
-                    float2 *__restrict__ probe_out)
+__device__ __forceinline__ void viscosity_predict_one(
+    int i, const Ctx &c, const DevState *__restrict__ st, const float2 *__restrict__ pos,
+    const float2 *__restrict__ vel, const int *__restrict__ start, bool capped,
+    float2 *__restrict__ pos_out, float2 *__restrict__ prev_out, uint2 *__restrict__ kr_out,
+    unsigned *__restrict__ cnt, float2 *__restrict__ probe_out)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (!PROBE && i == 0) *occ_reset = 0u;
-    if (i >= n) return;
-    const tunable_parameters P = *dP;
-    const float dt = P.time_step;
-    const float gdt = __fmul_rn(-P.g, dt);
-    const float hh = P.smoothing_radius;
+    const Scene *S = c.scenes + scene_of(c, i);
+    const SG g = load_grid(S);
+    const float dt = __ldg(&S->P.time_step);
+    const float gdt = __fmul_rn(-__ldg(&S->P.g), dt);
+    const float hh = __ldg(&S->P.smoothing_radius);
     const float h2 = __fmul_rn(hh, hh);
     const float h_recip = __fdiv_rn(1.0f, hh);
-    const float sigma = P.sigma, beta = P.beta;
-    const bool capped = *occ_in > (unsigned)g.max_bucket;
+    const float sigma = __ldg(&S->P.sigma), beta = __ldg(&S->P.beta);
 
     const float2 p = pos[i];
     float2 v = vel[i];
@@ -321,7 +321,7 @@ k_viscosity_predict(int n, Grid g, const tunable_parameters *__restrict__ dP,
             dvy -= 0.5f * clamp5(imp * qy * r_recip);
         }
     };
-    if ((PROBE || st->lists_valid) && searchable(key, i, start, g, capped)) {
+    if ((PROBE || st->lists_valid) && searchable(key, i, start, g, capped, c.max_bucket)) {
         bool walked = false;
         if (!capped) {
             // two phases: a cheap scan marks the neighbours of each stencil
@@ -357,7 +357,7 @@ k_viscosity_predict(int n, Grid g, const tunable_parameters *__restrict__ dP,
                 walked = true;
             }
         }
-        if (!walked) for_each_candidate(key, start, g, capped, impulse);
+        if (!walked) for_each_candidate(key, start, g, capped, c.max_bucket, impulse);
     }
     if (PROBE) {
         probe_out[i] = make_float2(dvx, dvy);
@@ -367,12 +367,35 @@ k_viscosity_predict(int n, Grid g, const tunable_parameters *__restrict__ dP,
     v.y = __fadd_rn(v.y, dvy);
     float nx = __fadd_rn(p.x, __fmul_rn(v.x, dt));
     float ny = __fadd_rn(p.y, __fmul_rn(v.y, dt));
-    boundary(nx, ny, P, g);
+    boundary_of(nx, ny, S);
     const unsigned k2 = cell_key(nx, ny, g);
     const unsigned rank = atomicAdd(cnt + k2, 1u);
     pos_out[i] = make_float2(nx, ny);
     prev_out[i] = p;
     kr_out[i] = make_uint2(k2, rank);
+}
+
+template <bool PROBE, bool PERSIST = false>
+__global__ void __launch_bounds__(kMaxBlock)
+k_viscosity_predict(Ctx c, const DevState *__restrict__ st, const float2 *__restrict__ pos,
+                    const float2 *__restrict__ vel, const int *__restrict__ start,
+                    const unsigned *__restrict__ occ_in, unsigned *occ_reset,
+                    float2 *__restrict__ pos_out, float2 *__restrict__ prev_out,
+                    uint2 *__restrict__ kr_out, unsigned *__restrict__ cnt,
+                    float2 *__restrict__ probe_out)
+{
+    const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (!PROBE && i0 == 0) *occ_reset = 0u;
+    const bool capped = *occ_in > (unsigned)c.max_bucket;
+    if (!PERSIST) {
+        if (i0 < c.n)
+            viscosity_predict_one<PROBE>(i0, c, st, pos, vel, start, capped, pos_out, prev_out,
+                                         kr_out, cnt, probe_out);
+        return;
+    }
+    for (int i = i0; i < c.n; i += gridDim.x * blockDim.x)
+        viscosity_predict_one<PROBE>(i, c, st, pos, vel, start, capped, pos_out, prev_out, kr_out,
+                                     cnt, probe_out);
 }
 
 // ---------------------------------------------------------------------------
@@ -385,23 +408,22 @@ k_viscosity_predict(int n, Grid g, const tunable_parameters *__restrict__ dP,
 // Writes xr = (x, y, rho, rho_near) and, per stencil row, the bit mask of the
 // candidates that are neighbours (r2 <= h2, self excluded), which the
 // relaxation pass of the same positions walks instead of the whole stencil.
-__global__ void __launch_bounds__(kBlock)
-k_density(int n, Grid g, const tunable_parameters *__restrict__ dP,
-          const float2 *__restrict__ pos, const int *__restrict__ start,
-          const unsigned *__restrict__ occ_in, float4 *__restrict__ xr_out,
-          ulonglong2 *__restrict__ mask01, unsigned long long *__restrict__ mask2)
+__device__ __forceinline__ void density_one(int i, const Ctx &c, const float2 *__restrict__ pos,
+                                            const int *__restrict__ start, bool capped,
+                                            float4 *__restrict__ xr_out,
+                                            ulonglong2 *__restrict__ mask01,
+                                            unsigned long long *__restrict__ mask2)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float hh = dP->smoothing_radius;
+    const Scene *S = c.scenes + scene_of(c, i);
+    const SG g = load_grid(S);
+    const float hh = __ldg(&S->P.smoothing_radius);
     const float h2 = __fmul_rn(hh, hh);
     const float h_recip = __fdiv_rn(1.0f, hh);
-    const bool capped = *occ_in > (unsigned)g.max_bucket;
     const float2 p = pos[i];
     const unsigned key = cell_key(p.x, p.y, g);
     float a = 0.0f, b = 0.0f;
     unsigned long long m[3] = {0ull, 0ull, 0ull};
-    if (searchable(key, i, start, g, capped)) {
+    if (searchable(key, i, start, g, capped, c.max_bucket)) {
         if (!capped) {
             int ra[3], rl[3];
             stencil_rows(key, start, g, ra, rl);
@@ -433,7 +455,7 @@ k_density(int n, Grid g, const tunable_parameters *__restrict__ dP,
             const int self = i - ra[1];
             if (self < kMaskRow) m[1] &= ~(1ull << self);
         } else {
-            for_each_candidate(key, start, g, true, [&](int j) {
+            for_each_candidate(key, start, g, true, c.max_bucket, [&](int j) {
                 if (j == i) return;
                 const float2 q = __ldg(pos + j);
                 const float r2 = dist2(p.x - q.x, p.y - q.y);
@@ -454,6 +476,33 @@ k_density(int n, Grid g, const tunable_parameters *__restrict__ dP,
     mask2[i] = m[2];
 }
 
+template <bool PERSIST>
+__global__ void __launch_bounds__(kMaxBlock)
+k_density_t(Ctx c, const float2 *__restrict__ pos, const int *__restrict__ start,
+            const unsigned *__restrict__ occ_in, float4 *__restrict__ xr_out,
+            ulonglong2 *__restrict__ mask01, unsigned long long *__restrict__ mask2)
+{
+    const bool capped = *occ_in > (unsigned)c.max_bucket;
+    const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (!PERSIST) {
+        if (i0 < c.n) density_one(i0, c, pos, start, capped, xr_out, mask01, mask2);
+        return;
+    }
+    for (int i = i0; i < c.n; i += gridDim.x * blockDim.x)
+        density_one(i, c, pos, start, capped, xr_out, mask01, mask2);
+}
+
+// One density launch per block (the form other translation units call).
+__global__ void __launch_bounds__(kMaxBlock)
+k_density(Ctx c, const float2 *__restrict__ pos, const int *__restrict__ start,
+          const unsigned *__restrict__ occ_in, float4 *__restrict__ xr_out,
+          ulonglong2 *__restrict__ mask01, unsigned long long *__restrict__ mask2)
+{
+    const bool capped = *occ_in > (unsigned)c.max_bucket;
+    const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i0 < c.n) density_one(i0, c, pos, start, capped, xr_out, mask01, mask2);
+}
+
 // ---------------------------------------------------------------------------
 // pass 3: relaxation (gather) + boundary + velocity update + cell key
 // ---------------------------------------------------------------------------
@@ -462,12 +511,13 @@ k_density(int n, Grid g, const tunable_parameters *__restrict__ dP,
 // its own half list in the reference: same cell and smaller id
 // (hash.c:178-199), or j's cell is one of i's forward cells
 // (0,+1), (+1,-1), (+1,0), (+1,+1) (hash.c:203-234).
-__device__ __noinline__ bool owns_pair(unsigned ki, int id_i, float2 qj, int id_j, const Grid &g)
+__device__ __noinline__ bool owns_pair(unsigned ki, int id_i, float2 qj, int id_j, const SG &g)
 {
     const unsigned kj = cell_key(qj.x, qj.y, g);
     if (kj == ki) return id_i < id_j;
-    const int yi = (int)(ki / (unsigned)g.size_x), xi = (int)ki - yi * g.size_x;
-    const int yj = (int)(kj / (unsigned)g.size_x), xj = (int)kj - yj * g.size_x;
+    const int li = (int)ki - g.c_off, lj = (int)kj - g.c_off;
+    const int yi = li / g.size_x, xi = li - yi * g.size_x;
+    const int yj = lj / g.size_x, xj = lj - yj * g.size_x;
     const int dx = xj - xi, dy = yj - yi;
     return (dx == 0 && dy == 1) || (dx == 1 && dy >= -1 && dy <= 1);
 }
@@ -479,7 +529,7 @@ struct RelaxConsts {
 // One neighbour's contribution to the displacement (r2 <= h2 known).
 __device__ __forceinline__ void relax_pair(const RelaxConsts &c, float2 p, float Pi, float Pni,
                                            float4 q, int i, int j, unsigned key,
-                                           const int *__restrict__ ids, const Grid &g, float &ax,
+                                           const int *__restrict__ ids, const SG &g, float &ax,
                                            float &ay, int &nudges)
 {
     const float ex = p.x - q.x, ey = p.y - q.y;
@@ -515,31 +565,25 @@ __device__ __forceinline__ void relax_pair(const RelaxConsts &c, float2 p, float
 // overflowing buckets) fall back to the whole stencil.
 // PROBE writes the displacement instead of advancing.
 template <bool PROBE>
-__global__ void __launch_bounds__(kBlock, 5)
-k_relax_update(int n, Grid g, const tunable_parameters *__restrict__ dP,
-               const float4 *__restrict__ xr, const ulonglong2 *__restrict__ mask01,
-               const unsigned long long *__restrict__ mask2, const float2 *__restrict__ prev,
-               const int *__restrict__ ids, const int *__restrict__ start,
-               const unsigned *__restrict__ occ_in, unsigned *occ_reset,
-               float2 *__restrict__ pos_out, float2 *__restrict__ vel_out,
-               uint2 *__restrict__ kr_out, unsigned *__restrict__ cnt,
-               float2 *__restrict__ probe_out)
+__device__ __forceinline__ void relax_update_one(
+    int i, const Ctx &cx, const float4 *__restrict__ xr, const ulonglong2 *__restrict__ mask01,
+    const unsigned long long *__restrict__ mask2, const float2 *__restrict__ prev,
+    const int *__restrict__ ids, const int *__restrict__ start, bool capped,
+    float2 *__restrict__ pos_out, float2 *__restrict__ vel_out, uint2 *__restrict__ kr_out,
+    unsigned *__restrict__ cnt, float2 *__restrict__ probe_out)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (!PROBE && i == 0) *occ_reset = 0u;
-    if (i >= n) return;
-    const tunable_parameters P = *dP;
+    const Scene *S = cx.scenes + scene_of(cx, i);
+    const SG g = load_grid(S);
     RelaxConsts c;
-    c.hh = P.smoothing_radius;
+    c.hh = __ldg(&S->P.smoothing_radius);
     c.h2 = __fmul_rn(c.hh, c.hh);
     c.h_recip = __fdiv_rn(1.0f, c.hh);
-    const float dt = P.time_step;
+    const float dt = __ldg(&S->P.time_step);
     c.dt2 = dt * dt;
-    c.k = P.k;
-    c.k_near = P.k_near;
-    c.rest = P.rest_density;
-    c.half_spring = 0.5f * P.k_spring;
-    const bool capped = *occ_in > (unsigned)g.max_bucket;
+    c.k = __ldg(&S->P.k);
+    c.k_near = __ldg(&S->P.k_near);
+    c.rest = __ldg(&S->P.rest_density);
+    c.half_spring = 0.5f * __ldg(&S->P.k_spring);
 
     const float4 me = xr[i];
     const float2 p = make_float2(me.x, me.y);
@@ -547,7 +591,7 @@ k_relax_update(int n, Grid g, const tunable_parameters *__restrict__ dP,
     const unsigned key = cell_key(p.x, p.y, g);
     float ax = 0.0f, ay = 0.0f;
     int nudges = 0;
-    if (searchable(key, i, start, g, capped)) {
+    if (searchable(key, i, start, g, capped, cx.max_bucket)) {
         bool walked = false;
         if (!capped) {
             int ra[3], rl[3];
@@ -569,7 +613,7 @@ k_relax_update(int n, Grid g, const tunable_parameters *__restrict__ dP,
             }
         }
         if (!walked) {
-            for_each_candidate(key, start, g, capped, [&](int j) {
+            for_each_candidate(key, start, g, capped, cx.max_bucket, [&](int j) {
                 if (j == i) return;
                 const float4 q = __ldg(xr + j);
                 if (dist2(p.x - q.x, p.y - q.y) > c.h2) return;
@@ -584,7 +628,7 @@ k_relax_update(int n, Grid g, const tunable_parameters *__restrict__ dP,
     }
     float nx = __fadd_rn(__fadd_rn(p.x, ax), nd);
     float ny = __fadd_rn(__fadd_rn(p.y, ay), nd);
-    boundary(nx, ny, P, g);
+    boundary_of(nx, ny, S);
     const float2 pv = prev[i];
     const float vx = clamp5(__fdiv_rn(__fsub_rn(nx, pv.x), dt));
     const float vy = clamp5(__fdiv_rn(__fsub_rn(ny, pv.y), dt));
@@ -595,29 +639,55 @@ k_relax_update(int n, Grid g, const tunable_parameters *__restrict__ dP,
     kr_out[i] = make_uint2(k2, rank);
 }
 
+template <bool PROBE, bool PERSIST = false>
+__global__ void __launch_bounds__(kBlock, 4)
+k_relax_update(Ctx c, const float4 *__restrict__ xr, const ulonglong2 *__restrict__ mask01,
+               const unsigned long long *__restrict__ mask2, const float2 *__restrict__ prev,
+               const int *__restrict__ ids, const int *__restrict__ start,
+               const unsigned *__restrict__ occ_in, unsigned *occ_reset,
+               float2 *__restrict__ pos_out, float2 *__restrict__ vel_out,
+               uint2 *__restrict__ kr_out, unsigned *__restrict__ cnt,
+               float2 *__restrict__ probe_out)
+{
+    const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (!PROBE && i0 == 0) *occ_reset = 0u;
+    const bool capped = *occ_in > (unsigned)c.max_bucket;
+    if (!PERSIST) {
+        if (i0 < c.n)
+            relax_update_one<PROBE>(i0, c, xr, mask01, mask2, prev, ids, start, capped, pos_out,
+                                    vel_out, kr_out, cnt, probe_out);
+        return;
+    }
+    for (int i = i0; i < c.n; i += gridDim.x * blockDim.x)
+        relax_update_one<PROBE>(i, c, xr, mask01, mask2, prev, ids, start, capped, pos_out,
+                                vel_out, kr_out, cnt, probe_out);
+}
+
 // ---------------------------------------------------------------------------
 // state I/O, diagnostics, neighbour lists
 // ---------------------------------------------------------------------------
 
 // Sorted state -> id order: out = [pos | vel | prev | rho | pressure] (5 n float2).
 __global__ void __launch_bounds__(kBlock)
-k_unpermute(int n, const tunable_parameters *__restrict__ dP, const int *__restrict__ id_a,
-            const float2 *__restrict__ pos_a, const float2 *__restrict__ vel_a,
-            const int *__restrict__ id_c, const float2 *__restrict__ prev_c,
-            const float4 *__restrict__ xr_c, float2 *__restrict__ out)
+k_unpermute(Ctx c, const int *__restrict__ id_a, const float2 *__restrict__ pos_a,
+            const float2 *__restrict__ vel_a, const int *__restrict__ id_c,
+            const float2 *__restrict__ prev_c, const float4 *__restrict__ xr_c,
+            float2 *__restrict__ out)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= c.n) return;
+    const size_t n = (size_t)c.n;
     const int ia = id_a[i], ic = id_c[i];
     out[ia] = pos_a[i];
-    out[(size_t)n + ia] = vel_a[i];
-    out[2 * (size_t)n + ic] = prev_c[i];
+    out[n + ia] = vel_a[i];
+    out[2 * n + ic] = prev_c[i];
     const float4 x4 = xr_c[i];
     const float2 r = make_float2(x4.z, x4.w);
-    out[3 * (size_t)n + ic] = r;
-    // pressure and near pressure, fluid.c:563-564
-    out[4 * (size_t)n + ic] = make_float2(__fmul_rn(dP->k, __fsub_rn(r.x, dP->rest_density)),
-                                          __fmul_rn(dP->k_near, r.y));
+    out[3 * n + ic] = r;
+    // pressure and near pressure, fluid.c:563-564, with the scene's tunables
+    const Scene *S = c.scenes + scene_of(c, i);
+    const float k = __ldg(&S->P.k), rest = __ldg(&S->P.rest_density), kn = __ldg(&S->P.k_near);
+    out[4 * n + ic] = make_float2(__fmul_rn(k, __fsub_rn(r.x, rest)), __fmul_rn(kn, r.y));
 }
 
 // (rho, rho_near) of the (x, y, rho, rho_near) records.
@@ -639,8 +709,7 @@ k_by_id(int n, const int *__restrict__ ids, const float2 *__restrict__ in, float
     out[ids[i]] = in[i];
 }
 
-// Uploaded id-order arrays into the *_c slots that download reads before the
-// first step (prev, densities), with the identity id map.
+// Identity id map for the *_c slots that download reads before the first step.
 __global__ void __launch_bounds__(kBlock)
 k_iota(int n, int *__restrict__ ids)
 {
@@ -650,11 +719,13 @@ k_iota(int n, int *__restrict__ ids)
 
 // Pixel-space shorts for the render rank (fluid.c:360-361), by id.
 __global__ void __launch_bounds__(kBlock)
-k_pack_coords(int n, float max_x, float max_y, const int *__restrict__ id_a,
-              const float2 *__restrict__ pos_a, short2 *__restrict__ out)
+k_pack_coords(Ctx c, const int *__restrict__ id_a, const float2 *__restrict__ pos_a,
+              short2 *__restrict__ out)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= c.n) return;
+    const Scene *S = c.scenes + scene_of(c, i);
+    const float max_x = __ldg(&S->max_x), max_y = __ldg(&S->max_y);
     const float2 p = pos_a[i];
     const float cx = __fmul_rn(__fsub_rn(__fdiv_rn(__fmul_rn(2.0f, p.x), max_x), 1.0f), 32767.0f);
     const float cy = __fmul_rn(__fsub_rn(__fdiv_rn(__fmul_rn(2.0f, p.y), max_y), 1.0f), 32767.0f);
@@ -702,58 +773,104 @@ __global__ void k_diag_final(int nparts, int n, const double *__restrict__ parti
     out[2] = n ? s2 / n : 0.0;
 }
 
+// Per-scene FP64 means (one block per scene, fixed order).  The density
+// records are in C order and the velocities in A order; both keep every
+// scene in its own slot range.
+__global__ void __launch_bounds__(kBlock)
+k_diag_scenes(Ctx c, const float4 *__restrict__ xr_c, const float2 *__restrict__ vel_a,
+              double *__restrict__ out)
+{
+    __shared__ double sh[3][kBlock / 32];
+    const int s = blockIdx.x;
+    const int b0 = __ldg(c.p_off + s), b1 = __ldg(c.p_off + s + 1);
+    double a = 0.0, b = 0.0, k = 0.0;
+    for (int i = b0 + threadIdx.x; i < b1; i += blockDim.x) {
+        const float4 r = xr_c[i];
+        const float2 v = vel_a[i];
+        a += r.z;
+        b += r.w;
+        k += 0.5 * ((double)v.x * v.x + (double)v.y * v.y);
+    }
+    a = warp_sum(a); b = warp_sum(b); k = warp_sum(k);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) { sh[0][warp] = a; sh[1][warp] = b; sh[2][warp] = k; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s0 = 0, s1 = 0, s2 = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { s0 += sh[0][w]; s1 += sh[1][w]; s2 += sh[2][w]; }
+        const int m = b1 - b0;
+        out[3 * s] = m ? s0 / m : 0.0;
+        out[3 * s + 1] = m ? s1 / m : 0.0;
+        out[3 * s + 2] = m ? s2 / m : 0.0;
+    }
+}
+
 // The reference's half list of one particle, in its order (hash.c:169-234):
 // later members of its own cell, then the forward cells (0,+1), (+1,-1),
 // (+1,0), (+1,+1), each in id order, r2 <= h2, cut at max_neighbors.
 // WRITE = false counts, WRITE = true writes ids at out + off[id].
 template <bool WRITE>
 __global__ void __launch_bounds__(kBlock)
-k_half_lists(int n, Grid g, const tunable_parameters *__restrict__ dP,
-             const float2 *__restrict__ pos, const int *__restrict__ ids,
+k_half_lists(Ctx c, const float2 *__restrict__ pos, const int *__restrict__ ids,
              const int *__restrict__ start, const unsigned *__restrict__ occ_in,
              unsigned *__restrict__ counts, const int *__restrict__ off, int *__restrict__ out)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float hh = dP->smoothing_radius;
+    if (i >= c.n) return;
+    const Scene *S = c.scenes + scene_of(c, i);
+    const SG g = load_grid(S);
+    const float hh = __ldg(&S->P.smoothing_radius);
+    const int max_neighbors = __ldg(&S->max_neighbors);
     const float h2 = __fmul_rn(hh, hh);
-    const bool capped = *occ_in > (unsigned)g.max_bucket;
+    const bool capped = *occ_in > (unsigned)c.max_bucket;
     const float2 p = pos[i];
     const unsigned key = cell_key(p.x, p.y, g);
     const int myid = ids[i];
-    int c = 0;
+    int cnum = 0;
     int *dst = WRITE ? out + off[myid] : nullptr;
-    if (searchable(key, i, start, g, capped)) {
-        const int gy = (int)(key / (unsigned)g.size_x), gx = (int)key - gy * g.size_x;
-        const int fdx[5] = {0, 0, 1, 1, 1}, fdy[5] = {0, 1, -1, 0, 1};
+    if (searchable(key, i, start, g, capped, c.max_bucket)) {
+        const int lk = (int)key - g.c_off;
+        const int gy = lk / g.size_x, gx = lk - gy * g.size_x;
+#pragma unroll
         for (int f = 0; f < 5; ++f) {
-            const int x = gx + fdx[f], y = gy + fdy[f];
+            const int x = gx + (f >= 2 ? 1 : 0);
+            const int y = gy + (f == 0 ? 0 : (f == 1 ? 1 : f - 3));
             if (x < 0 || y < 0 || x >= g.size_x || y >= g.size_y) continue;
-            const int cell = y * g.size_x + x;
+            const int cell = g.c_off + y * g.size_x + x;
             const int a = start[cell], e = start[cell + 1];
-            const int b = capped && e - a > g.max_bucket ? a + g.max_bucket : e;
+            const int b = capped && e - a > c.max_bucket ? a + c.max_bucket : e;
             for (int j = f == 0 ? i + 1 : a; j < b; ++j) {
                 const float2 q = pos[j];
                 if (dist2(p.x - q.x, p.y - q.y) > h2) continue;
-                if (c < g.max_neighbors) {
-                    if (WRITE) dst[c] = ids[j];
-                    ++c;
+                if (cnum < max_neighbors) {
+                    if (WRITE) dst[cnum] = ids[j];
+                    ++cnum;
                 }
             }
         }
     }
-    if (!WRITE) counts[myid] = (unsigned)c;
+    if (!WRITE) counts[myid] = (unsigned)cnum;
 }
 
 // ---------------------------------------------------------------------------
 // host-side launchers
 // ---------------------------------------------------------------------------
 
-static inline int blocks_for(int n) { return (n + kBlock - 1) / kBlock; }
+static inline int blocks_for(int n, int bs = kBlock) { return (n + bs - 1) / bs; }
+
+// Grid of a gather launch for shape s.
+static inline dim3 gather_grid(const sph_cuda *h, const Shape &s)
+{
+    const int tiles = blocks_for(h->n, s.block);
+    if (s.persistent <= 0) return dim3(tiles);
+    const int p = h->num_sms * s.persistent;
+    return dim3(p < tiles ? p : tiles);
+}
 
 // Exclusive scan of `in` (M entries) into out (M + 1 entries).  Both arrays
 // must be 16-byte aligned: the scan kernels move 16-byte vectors.
-static int launch_scan(sph_cuda *h, unsigned *in, int M, int *out, unsigned *occ, bool zero)
+static int launch_scan(sph_cuda *h, unsigned *in, int M, int *out, unsigned *occ, bool zero,
+                       const unsigned *nocell)
 {
     if (((uintptr_t)in | (uintptr_t)out) & 15u) {
         set_error("internal: scan arrays not 16-byte aligned");
@@ -764,9 +881,8 @@ static int launch_scan(sph_cuda *h, unsigned *in, int M, int *out, unsigned *occ
         set_error("internal: scan of %d items exceeds the tile buffer", M);
         return SPH_ERR_INVALID;
     }
-    k_scan_reduce<<<tiles, kScanThreads, 0, h->stream>>>(in, M, h->g.ncells, h->tile_sums,
-                                                         h->d_state, occ, h->g.max_bucket,
-                                                         h->g.max_neighbors);
+    k_scan_reduce<<<tiles, kScanThreads, 0, h->stream>>>(in, M, nocell, h->tile_sums, h->d_state,
+                                                         occ, h->max_bucket, h->max_neighbors);
     k_scan_apply<<<tiles, kScanThreads, 0, h->stream>>>(in, M, h->tile_sums, out, zero ? 1 : 0);
     return SPH_OK;
 }
@@ -783,8 +899,9 @@ int enqueue_step(sph_cuda *h, cudaEvent_t *events, int *nkernels)
 {
     const int n = h->n;
     const int nb = blocks_for(n);
-    const int M = h->g.ncells + 1;
+    const int M = h->M;
     const int tiles = (M + kScanTile - 1) / kScanTile;
+    const Ctx c = make_ctx(h);
     DevState *st = h->d_state;
     int e = 0;
     auto mark = [&]() {
@@ -792,13 +909,17 @@ int enqueue_step(sph_cuda *h, cudaEvent_t *events, int *nkernels)
         ++e;
     };
     mark();
-    k_viscosity_predict<false><<<nb, kBlock, 0, h->stream>>>(
-        n, h->g, h->d_params, st, h->pos_a, h->vel_a, h->start_a, &st->build_max_occ[SLOT_RELAXED],
-        &st->build_max_occ[SLOT_PREDICTED], h->pos_b, h->prev_b, h->kr_b, h->cnt, nullptr);
+    {
+        auto kv = h->shape[0].persistent ? k_viscosity_predict<false, true>
+                                         : k_viscosity_predict<false, false>;
+        kv<<<gather_grid(h, h->shape[0]), h->shape[0].block, 0, h->stream>>>(
+            c, st, h->pos_a, h->vel_a, h->start_a, &st->build_max_occ[SLOT_RELAXED],
+            &st->build_max_occ[SLOT_PREDICTED], h->pos_b, h->prev_b, h->kr_b, h->cnt, nullptr);
+    }
     mark();
-    k_scan_reduce<<<tiles, kScanThreads, 0, h->stream>>>(h->cnt, M, h->g.ncells, h->tile_sums, st,
+    k_scan_reduce<<<tiles, kScanThreads, 0, h->stream>>>(h->cnt, M, h->d_nocell, h->tile_sums, st,
                                                          &st->build_max_occ[SLOT_PREDICTED],
-                                                         h->g.max_bucket, h->g.max_neighbors);
+                                                         h->max_bucket, h->max_neighbors);
     mark();
     k_scan_apply<<<tiles, kScanThreads, 0, h->stream>>>(h->cnt, M, h->tile_sums, h->start_c, 1);
     mark();
@@ -807,18 +928,24 @@ int enqueue_step(sph_cuda *h, cudaEvent_t *events, int *nkernels)
     k_permute<<<nb, kBlock, 0, h->stream>>>(n, h->kr_b, h->start_c, h->tmp_id, h->id_a, h->pos_b,
                                             h->prev_b, h->id_c, h->pos_c, h->prev_c, nullptr);
     mark();
-    k_density<<<nb, kBlock, 0, h->stream>>>(n, h->g, h->d_params, h->pos_c, h->start_c,
-                                            &st->build_max_occ[SLOT_PREDICTED], h->xr_c,
-                                            h->mask01_c, h->mask2_c);
+    {
+        auto kd = h->shape[1].persistent ? k_density_t<true> : k_density_t<false>;
+        kd<<<gather_grid(h, h->shape[1]), h->shape[1].block, 0, h->stream>>>(
+            c, h->pos_c, h->start_c, &st->build_max_occ[SLOT_PREDICTED], h->xr_c, h->mask01_c,
+            h->mask2_c);
+    }
     mark();
-    k_relax_update<false><<<nb, kBlock, 0, h->stream>>>(
-        n, h->g, h->d_params, h->xr_c, h->mask01_c, h->mask2_c, h->prev_c, h->id_c, h->start_c,
-        &st->build_max_occ[SLOT_PREDICTED], &st->build_max_occ[SLOT_RELAXED], h->pos_b, h->vel_b,
-        h->kr_b, h->cnt, nullptr);
+    {
+        auto kr = h->shape[2].persistent ? k_relax_update<false, true> : k_relax_update<false, false>;
+        kr<<<gather_grid(h, h->shape[2]), h->shape[2].block, 0, h->stream>>>(
+            c, h->xr_c, h->mask01_c, h->mask2_c, h->prev_c, h->id_c, h->start_c,
+            &st->build_max_occ[SLOT_PREDICTED], &st->build_max_occ[SLOT_RELAXED], h->pos_b,
+            h->vel_b, h->kr_b, h->cnt, nullptr);
+    }
     mark();
-    k_scan_reduce<<<tiles, kScanThreads, 0, h->stream>>>(h->cnt, M, h->g.ncells, h->tile_sums, st,
+    k_scan_reduce<<<tiles, kScanThreads, 0, h->stream>>>(h->cnt, M, h->d_nocell, h->tile_sums, st,
                                                          &st->build_max_occ[SLOT_RELAXED],
-                                                         h->g.max_bucket, h->g.max_neighbors);
+                                                         h->max_bucket, h->max_neighbors);
     mark();
     k_scan_apply<<<tiles, kScanThreads, 0, h->stream>>>(h->cnt, M, h->tile_sums, h->start_a, 1);
     mark();
@@ -837,7 +964,6 @@ const char *kernel_name(int k)
 }
 int step_kernel_count() { return kStepKernels; }
 
-
 // Upload tail: pos_b / vel_b (id order) -> sorted A state; prev_c / xr_c
 // already hold the uploaded values in id order.
 int upload_soa_device(sph_cuda *h, int n)
@@ -846,10 +972,10 @@ int upload_soa_device(sph_cuda *h, int n)
     DevState *st = h->d_state;
     if (n > 0) {
         k_iota<<<nb, kBlock, 0, h->stream>>>(n, h->id_c);
-        k_keys<<<nb, kBlock, 0, h->stream>>>(n, h->g, h->pos_b, h->kr_b, h->cnt,
+        k_keys<<<nb, kBlock, 0, h->stream>>>(make_ctx(h), h->pos_b, h->kr_b, h->cnt,
                                              &st->build_max_occ[SLOT_RELAXED]);
-        const int rc = launch_scan(h, h->cnt, h->g.ncells + 1, h->start_a,
-                                   &st->build_max_occ[SLOT_RELAXED], true);
+        const int rc = launch_scan(h, h->cnt, h->M, h->start_a, &st->build_max_occ[SLOT_RELAXED],
+                                   true, h->d_nocell);
         if (rc != SPH_OK) return rc;
         k_scatter_ids<<<nb, kBlock, 0, h->stream>>>(n, h->kr_b, nullptr, h->start_a, h->tmp_id);
         k_permute<<<nb, kBlock, 0, h->stream>>>(n, h->kr_b, h->start_a, h->tmp_id, nullptr,
@@ -862,7 +988,7 @@ int upload_soa_device(sph_cuda *h, int n)
 int launch_unpermute(sph_cuda *h, float2 *out)
 {
     if (h->n == 0) return SPH_OK;
-    k_unpermute<<<blocks_for(h->n), kBlock, 0, h->stream>>>(h->n, h->d_params, h->id_a, h->pos_a,
+    k_unpermute<<<blocks_for(h->n), kBlock, 0, h->stream>>>(make_ctx(h), h->id_a, h->pos_a,
                                                             h->vel_a, h->id_c, h->prev_c, h->xr_c,
                                                             out);
     return cuda_fail(cudaGetLastError(), "unpermute");
@@ -871,8 +997,7 @@ int launch_unpermute(sph_cuda *h, float2 *out)
 int launch_pack(sph_cuda *h, short2 *out)
 {
     if (h->n == 0) return SPH_OK;
-    k_pack_coords<<<blocks_for(h->n), kBlock, 0, h->stream>>>(h->n, h->g.max_x, h->g.max_y,
-                                                              h->id_a, h->pos_a, out);
+    k_pack_coords<<<blocks_for(h->n), kBlock, 0, h->stream>>>(make_ctx(h), h->id_a, h->pos_a, out);
     return cuda_fail(cudaGetLastError(), "pack coords");
 }
 
@@ -882,6 +1007,13 @@ int launch_diagnostics(sph_cuda *h, double *d_out)
     k_diag_partial<<<parts, kBlock, 0, h->stream>>>(h->n, h->xr_c, h->vel_a, h->d_partials);
     k_diag_final<<<1, 32, 0, h->stream>>>(parts, h->n, h->d_partials, d_out);
     return cuda_fail(cudaGetLastError(), "diagnostics");
+}
+
+int launch_scene_diagnostics(sph_cuda *h, double *d_out)
+{
+    if (h->nscenes == 0) return SPH_OK;
+    k_diag_scenes<<<h->nscenes, kBlock, 0, h->stream>>>(make_ctx(h), h->xr_c, h->vel_a, d_out);
+    return cuda_fail(cudaGetLastError(), "scene diagnostics");
 }
 
 // Probes on the A state.  which: 0 density, 1 relaxation displacement,
@@ -898,6 +1030,7 @@ int launch_probe(sph_cuda *h, int which, void *scratch, float2 *out)
     const int n = h->n;
     if (n == 0) return SPH_OK;
     const int nb = blocks_for(n);
+    const Ctx c = make_ctx(h);
     DevState *st = h->d_state;
     const unsigned *occ = &st->build_max_occ[SLOT_RELAXED];
     const size_t a = ((size_t)n * 16 + 255) & ~(size_t)255;
@@ -907,40 +1040,39 @@ int launch_probe(sph_cuda *h, int which, void *scratch, float2 *out)
     unsigned long long *m2 = (unsigned long long *)(base + 2 * a);
     float2 *sorted = (float2 *)(base + 3 * a);
     if (which == 0 || which == 1) {
-        k_density<<<nb, kBlock, 0, h->stream>>>(n, h->g, h->d_params, h->pos_a, h->start_a, occ, xr,
-                                                m01, m2);
+        k_density<<<nb, kBlock, 0, h->stream>>>(c, h->pos_a, h->start_a, occ, xr, m01, m2);
         if (which == 1)
             k_relax_update<true><<<nb, kBlock, 0, h->stream>>>(
-                n, h->g, h->d_params, xr, m01, m2, nullptr, h->id_a, h->start_a, occ, nullptr,
-                nullptr, nullptr, nullptr, nullptr, sorted);
+                c, xr, m01, m2, nullptr, h->id_a, h->start_a, occ, nullptr, nullptr, nullptr,
+                nullptr, nullptr, sorted);
         else
             k_xr_density<<<nb, kBlock, 0, h->stream>>>(n, xr, sorted);
     } else {
         k_viscosity_predict<true><<<nb, kBlock, 0, h->stream>>>(
-            n, h->g, h->d_params, st, h->pos_a, h->vel_a, h->start_a, occ, nullptr, nullptr,
-            nullptr, nullptr, nullptr, sorted);
+            c, st, h->pos_a, h->vel_a, h->start_a, occ, nullptr, nullptr, nullptr, nullptr,
+            nullptr, sorted);
     }
     k_by_id<<<nb, kBlock, 0, h->stream>>>(n, h->id_a, sorted, out);
     return cuda_fail(cudaGetLastError(), "probe");
 }
 
 // Half lists in the reference's order on the A state.  d_counts: n + 1
-// words (scanned in place into offsets), d_off: n + 1 ints.
+// words, d_off: n + 1 ints (both 16-byte aligned).
 int launch_half_lists(sph_cuda *h, unsigned *d_counts, int *d_off, int *d_ids, bool write)
 {
     const int n = h->n;
     if (n == 0) return SPH_OK;
     const int nb = blocks_for(n);
+    const Ctx c = make_ctx(h);
     const unsigned *occ = &h->d_state->build_max_occ[SLOT_RELAXED];
     if (!write) {
-        k_half_lists<false><<<nb, kBlock, 0, h->stream>>>(n, h->g, h->d_params, h->pos_a, h->id_a,
-                                                          h->start_a, occ, d_counts, nullptr,
-                                                          nullptr);
-        const int rc = launch_scan(h, d_counts, n, d_off, nullptr, false);
+        k_half_lists<false><<<nb, kBlock, 0, h->stream>>>(c, h->pos_a, h->id_a, h->start_a, occ,
+                                                          d_counts, nullptr, nullptr);
+        const int rc = launch_scan(h, d_counts, n, d_off, nullptr, false, nullptr);
         if (rc != SPH_OK) return rc;
     } else {
-        k_half_lists<true><<<nb, kBlock, 0, h->stream>>>(n, h->g, h->d_params, h->pos_a, h->id_a,
-                                                         h->start_a, occ, nullptr, d_off, d_ids);
+        k_half_lists<true><<<nb, kBlock, 0, h->stream>>>(c, h->pos_a, h->id_a, h->start_a, occ,
+                                                         nullptr, d_off, d_ids);
     }
     return cuda_fail(cudaGetLastError(), "half lists");
 }

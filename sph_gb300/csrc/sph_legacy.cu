@@ -69,15 +69,7 @@ int prepare(LegacyCtx &c, size_t dev_bytes, size_t host_bytes)
     return SPH_OK;
 }
 
-Grid box_grid(const AABB_t *b)
-{
-    Grid g{};
-    g.min_x = b->min_x;
-    g.max_x = b->max_x;
-    g.min_y = b->min_y;
-    g.max_y = b->max_y;
-    return g;
-}
+float4 box_grid(const AABB_t *b) { return make_float4(b->min_x, b->max_x, b->min_y, b->max_y); }
 
 inline int blocks(int n) { return (n + kBlock - 1) / kBlock; }
 
@@ -91,7 +83,7 @@ __global__ void kl_gravity(int n, float g, float dt, float2 *vel, float2 *rho)
     rho[i] = make_float2(0.0f, 0.0f);
 }
 
-__global__ void kl_predict(int n, tunable_parameters P, Grid g, float2 *pos, const float2 *vel,
+__global__ void kl_predict(int n, tunable_parameters P, float4 g, float2 *pos, const float2 *vel,
                            float2 *prev)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -105,7 +97,7 @@ __global__ void kl_predict(int n, tunable_parameters P, Grid g, float2 *pos, con
 }
 
 // updateVelocity (fluid.c:627-639), after boundaryConditions when `bc`.
-__global__ void kl_velocity(int n, tunable_parameters P, Grid g, int bc, float2 *pos,
+__global__ void kl_velocity(int n, tunable_parameters P, float4 g, int bc, float2 *pos,
                             const float2 *prev, float2 *vel)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -118,7 +110,7 @@ __global__ void kl_velocity(int n, tunable_parameters P, Grid g, int bc, float2 
                          clamp5(__fdiv_rn(__fsub_rn(y, q.y), P.time_step)));
 }
 
-__global__ void kl_boundary(tunable_parameters P, Grid g, float2 *pos)
+__global__ void kl_boundary(tunable_parameters P, float4 g, float2 *pos)
 {
     float x = pos->x, y = pos->y;
     boundary(x, y, P, g);
@@ -654,7 +646,7 @@ void updateVelocity(fluid_particle *p, param *params)
         float2 *dp = carve<float2>(d, 1), *dq = carve<float2>(d, 1), *dv = carve<float2>(d, 1);
         LTRY(cuda_fail(cudaMemcpyAsync(dp, &h[0], sizeof(float2), cudaMemcpyHostToDevice, c.stream), "H2D"));
         LTRY(cuda_fail(cudaMemcpyAsync(dq, &h[1], sizeof(float2), cudaMemcpyHostToDevice, c.stream), "H2D"));
-        kl_velocity<<<1, 32, 0, c.stream>>>(1, params->tunable_params, Grid{}, 0, dp, dq, dv);
+        kl_velocity<<<1, 32, 0, c.stream>>>(1, params->tunable_params, float4{}, 0, dp, dq, dv);
         LTRY(cuda_fail(cudaMemcpyAsync(&h[2], dv, sizeof(float2), cudaMemcpyDeviceToHost, c.stream), "D2H"));
         LTRY(sync(c));
         p->v_x = h[2].x;

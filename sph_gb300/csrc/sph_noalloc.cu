@@ -17,11 +17,12 @@
 namespace sph {
 
 // Kernels of sph_kernels.cu, launched here unchanged.
-__global__ void k_keys(int n, Grid g, const float2 *__restrict__ pos, uint2 *__restrict__ kr,
+__global__ void k_keys(Ctx c, const float2 *__restrict__ pos, uint2 *__restrict__ kr,
                        unsigned *__restrict__ cnt, unsigned *occ_reset);
-__global__ void k_scan_reduce(const unsigned *__restrict__ in, int M, int ncells,
-                              int *__restrict__ tile_sums, DevState *__restrict__ st,
-                              unsigned *occ, int max_bucket, int max_neighbors);
+__global__ void k_scan_reduce(const unsigned *__restrict__ in, int M,
+                              const unsigned *__restrict__ nocell, int *__restrict__ tile_sums,
+                              DevState *__restrict__ st, unsigned *occ, int max_bucket,
+                              int max_neighbors);
 __global__ void k_scan_apply(unsigned *__restrict__ in, int M, const int *__restrict__ tile_sums,
                              int *__restrict__ out, int zero_input);
 __global__ void k_scatter_ids(int n, const uint2 *__restrict__ kr, const int *__restrict__ id_src,
@@ -31,8 +32,7 @@ __global__ void k_permute(int n, const uint2 *__restrict__ kr, const int *__rest
                           const float2 *__restrict__ a_src, const float2 *__restrict__ b_src,
                           int *__restrict__ id_dst, float2 *__restrict__ a_dst,
                           float2 *__restrict__ b_dst, DevState *__restrict__ end_step);
-__global__ void k_density(int n, Grid g, const tunable_parameters *__restrict__ dP,
-                          const float2 *__restrict__ pos, const int *__restrict__ start,
+__global__ void k_density(Ctx c, const float2 *__restrict__ pos, const int *__restrict__ start,
                           const unsigned *__restrict__ occ_in, float4 *__restrict__ xr_out,
                           ulonglong2 *__restrict__ mask01, unsigned long long *__restrict__ mask2);
 
@@ -46,8 +46,11 @@ constexpr size_t kC = SPH_STATIC_MAX_CELLS;
 constexpr size_t kTiles = ((kC + 1 > kN ? kC + 1 : kN) + 1 + kScanTile - 1) / kScanTile;
 
 // Layout of the scratch array (byte offsets, each 256-byte aligned).
-constexpr size_t kOffParams = 0;
-constexpr size_t kOffState = kOffParams + up(sizeof(tunable_parameters));
+constexpr size_t kNocellWords = (kC + 1 + 31) / 32 + 1;
+constexpr size_t kOffScene = 0;
+constexpr size_t kOffPoff = kOffScene + up(sizeof(Scene));
+constexpr size_t kOffNocell = kOffPoff + up(2 * sizeof(int));
+constexpr size_t kOffState = kOffNocell + up(kNocellWords * sizeof(unsigned));
 constexpr size_t kOffCnt = kOffState + up(sizeof(DevState));
 constexpr size_t kOffStart = kOffCnt + up((kC + 1) * sizeof(unsigned));
 constexpr size_t kOffTiles = kOffStart + up((kC + 2) * sizeof(int));
@@ -94,11 +97,16 @@ int scratch_address(void **out)
     return SPH_OK;
 }
 
-// The smoothing radius is the only tunable the density pass reads.
-__global__ void k_static_params(float smoothing_radius)
+// The one-scene table of the call: scene record, slot offsets {0, n} and
+// the scene's no-cell bucket in the (cleared) no-cell bitmap.
+__global__ void k_static_scene(Scene s)
 {
-    tunable_parameters *p = reinterpret_cast<tunable_parameters *>(g_static_scratch + kOffParams);
-    p->smoothing_radius = smoothing_radius;
+    *reinterpret_cast<Scene *>(g_static_scratch + kOffScene) = s;
+    int *p_off = reinterpret_cast<int *>(g_static_scratch + kOffPoff);
+    p_off[0] = 0;
+    p_off[1] = s.n;
+    unsigned *bits = reinterpret_cast<unsigned *>(g_static_scratch + kOffNocell);
+    bits[s.ncells >> 5] |= 1u << (s.ncells & 31);
 }
 
 __global__ void __launch_bounds__(kBlock)
@@ -164,7 +172,9 @@ extern "C" int sph_cuda_density_static(const float *x, const float *y, int n,
     if (n == 0) return SPH_OK;
 
     char *base = static_cast<char *>(base_v);
-    tunable_parameters *params = reinterpret_cast<tunable_parameters *>(base + kOffParams);
+    const Scene *scene = reinterpret_cast<const Scene *>(base + kOffScene);
+    const int *p_off = reinterpret_cast<const int *>(base + kOffPoff);
+    unsigned *nocell = reinterpret_cast<unsigned *>(base + kOffNocell);
     DevState *state = reinterpret_cast<DevState *>(base + kOffState);
     unsigned *cnt = reinterpret_cast<unsigned *>(base + kOffCnt);
     int *start = reinterpret_cast<int *>(base + kOffStart);
@@ -178,16 +188,26 @@ extern "C" int sph_cuda_density_static(const float *x, const float *y, int n,
     ulonglong2 *m01 = reinterpret_cast<ulonglong2 *>(base + kOffM01);
     unsigned long long *m2 = reinterpret_cast<unsigned long long *>(base + kOffM2);
 
-    Grid g{};
-    g.spacing = grid->spacing;
-    g.size_x = (int)grid->size_x;
-    g.size_y = (int)grid->size_y;
-    g.ncells = (int)cells;
-    g.max_bucket = (int)grid->max_bucket_size;
-    g.max_neighbors = (int)grid->max_neighbors;
+    Scene sc{};
+    sc.P = *tp;
+    sc.spacing = grid->spacing;
+    sc.size_x = (int)grid->size_x;
+    sc.size_y = (int)grid->size_y;
+    sc.ncells = (int)cells;
+    sc.c_off = 0;
+    sc.p_off = 0;
+    sc.n = n;
+    sc.max_bucket = (int)grid->max_bucket_size;
+    sc.max_neighbors = (int)grid->max_neighbors;
+    Ctx c;
+    c.scenes = scene;
+    c.p_off = p_off;
+    c.nscenes = 1;
+    c.n = n;
+    c.max_bucket = sc.max_bucket;
 
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    const int M = g.ncells + 1;
+    const int M = sc.ncells + 1;
     const int nt = (M + kScanTile - 1) / kScanTile;
     const int nb = (n + kBlock - 1) / kBlock;
     // The array keeps the previous call's contents: the histogram and the
@@ -196,17 +216,20 @@ extern "C" int sph_cuda_density_static(const float *x, const float *y, int n,
     if (rc != SPH_OK) return rc;
     rc = cuda_fail(cudaMemsetAsync(state, 0, sizeof(DevState), s), "cudaMemsetAsync");
     if (rc != SPH_OK) return rc;
+    rc = cuda_fail(cudaMemsetAsync(nocell, 0, ((size_t)M + 31) / 32 * sizeof(unsigned), s),
+                   "cudaMemsetAsync");
+    if (rc != SPH_OK) return rc;
     unsigned *occ = &state->build_max_occ[SLOT_PROBE];
-    k_static_params<<<1, 1, 0, s>>>(tp->smoothing_radius);
+    k_static_scene<<<1, 1, 0, s>>>(sc);
     k_static_gather<<<nb, kBlock, 0, s>>>(n, x, y, pos_in);
-    k_keys<<<nb, kBlock, 0, s>>>(n, g, pos_in, kr, cnt, occ);
-    k_scan_reduce<<<nt, kScanThreads, 0, s>>>(cnt, M, g.ncells, tiles, state, occ, g.max_bucket,
-                                              g.max_neighbors);
+    k_keys<<<nb, kBlock, 0, s>>>(c, pos_in, kr, cnt, occ);
+    k_scan_reduce<<<nt, kScanThreads, 0, s>>>(cnt, M, nocell, tiles, state, occ, sc.max_bucket,
+                                              sc.max_neighbors);
     k_scan_apply<<<nt, kScanThreads, 0, s>>>(cnt, M, tiles, start, 1);
     k_scatter_ids<<<nb, kBlock, 0, s>>>(n, kr, nullptr, start, tmp);
     k_permute<<<nb, kBlock, 0, s>>>(n, kr, start, tmp, nullptr, pos_in, nullptr, id_s, pos_s,
                                     nullptr, nullptr);
-    k_density<<<nb, kBlock, 0, s>>>(n, g, params, pos_s, start, occ, xr, m01, m2);
+    k_density<<<nb, kBlock, 0, s>>>(c, pos_s, start, occ, xr, m01, m2);
     k_static_scatter<<<nb, kBlock, 0, s>>>(n, id_s, xr, density, density_near);
     return cuda_fail(cudaGetLastError(), "sph_cuda_density_static launch");
 }

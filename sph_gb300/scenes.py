@@ -180,6 +180,51 @@ def config2(n: int = 4_194_304) -> Scene:
     return sc
 
 
+def ensemble_scene(seed: int, name: str, n_range=(1024, 65536)) -> Scene:
+    """One scene of the batched ensemble: N = round(exp U(ln lo, ln hi))
+    particles; box aspect a ~ U[1, 4] and fill fraction f ~ U[0.2, 0.5] give a
+    box of area 0.25 N / f, W = sqrt(area a), H = W / a; the fluid is a
+    lattice block (spacing 0.5h, jitter 0.01h) filling a rectangle of the
+    box's aspect scaled by sqrt(f), at a uniform random position in the box;
+    k ~ U[0.1, 0.5], k_near ~ U[1, 3], sigma ~ U[0, 1], the rest as the dam
+    break; no mover.  Scene randoms use counters 0..7 of the seed, the jitter
+    counters 8 onward."""
+    u = uniform(seed, np.arange(8, dtype=np.uint64))
+    lo, hi = math.log(n_range[0]), math.log(n_range[1])
+    n = int(round(math.exp(lo + (hi - lo) * u[0])))
+    a = 1.0 + 3.0 * u[1]
+    f = 0.2 + 0.3 * u[2]
+    area = 0.25 * n / f
+    w = math.sqrt(area * a)
+    h_box = w / a
+    fw, fh = w * math.sqrt(f), h_box * math.sqrt(f)
+    x0, y0 = u[6] * (w - fw), u[7] * (h_box - fh)
+    cols = max(1, int(fw / 0.5))
+    p = Params(k=0.1 + 0.4 * u[3], k_near=1.0 + 2.0 * u[4], sigma=float(u[5]))
+    i = np.arange(n, dtype=np.int64)
+    row, col = np.divmod(i, cols)
+    ju = uniform(seed, np.arange(8, 8 + 2 * n, dtype=np.uint64)).reshape(n, 2)
+    x = (x0 + col * 0.5 + (ju[:, 0] * 2.0 - 1.0) * 0.01).astype(np.float32)
+    y = (y0 + row * 0.5 + (ju[:, 1] * 2.0 - 1.0) * 0.01).astype(np.float32)
+    bw, bh = np.float32(w), np.float32(h_box)
+    p.node_start_x, p.node_end_x = 0.0, float(bw)
+    sc = Scene(name=name, x=x, y=y, vx=np.zeros(n, np.float32), vy=np.zeros(n, np.float32),
+               box=(0.0, float(bw), 0.0, float(bh)), params=p, spacing=1.0,
+               size_x=int(math.ceil(float(bw))), size_y=int(math.ceil(float(bh))))
+    sc.meta = dict(aspect=a, fill=f)
+    return sc
+
+
+def config3(nscenes: int = 512, n_range=(1024, 65536)) -> list:
+    """The batched ensemble: 512 scenes (seeds 3000 + s), 500 steps."""
+    out = []
+    for s in range(nscenes):
+        sc = ensemble_scene(3000 + s, f"ensemble_{s}", n_range)
+        sc.steps = 500
+        out.append(sc)
+    return out
+
+
 def algorithmic_bytes_per_step(n: int, cells: int) -> int:
     """Canonical algorithmic HBM bytes of one step: 216 B per particle
     (viscosity+predict 40, cell build on predicted positions 68, density 16,

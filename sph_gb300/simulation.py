@@ -117,6 +117,25 @@ class Simulation:
         t = tunables(params or self.params)
         check(lib().sph_cuda_step(self._h, ctypes.byref(t), int(nsteps)))
 
+    def set_scene_params(self, scene: int, params: dict):
+        check(lib().sph_cuda_set_scene_params(self._h, int(scene), ctypes.byref(tunables(params))))
+
+    def autotune(self, trial_steps: int = 3) -> list:
+        """Picks the fastest launch shape per gather kernel (advances the
+        simulation by 8 * trial_steps steps); returns the 6 shape ints."""
+        out = (ctypes.c_int * 6)()
+        check(lib().sph_cuda_autotune(self._h, int(trial_steps), out))
+        return list(out)
+
+    def launch_shapes(self) -> list:
+        out = (ctypes.c_int * 6)()
+        check(lib().sph_cuda_get_launch_shapes(self._h, out))
+        return list(out)
+
+    def set_launch_shapes(self, shapes):
+        arr = (ctypes.c_int * 6)(*[int(v) for v in shapes])
+        check(lib().sph_cuda_set_launch_shapes(self._h, arr))
+
     def step_schedule(self, params_list: list):
         arr = (_lib.TunableParameters * len(params_list))(*[tunables(p) for p in params_list])
         check(lib().sph_cuda_step_schedule(self._h, arr, len(params_list)))
@@ -128,6 +147,13 @@ class Simulation:
         check(lib().sph_cuda_synchronize(self._h))
 
     # -- inspection ------------------------------------------------------------
+    def scene_diagnostics(self) -> np.ndarray:
+        """[nscenes, 3]: mean density, mean near density, kinetic energy per particle."""
+        ns = int(lib().sph_cuda_num_scenes(self._h))
+        out = np.zeros((ns, 3), np.float64)
+        check(lib().sph_cuda_scene_diagnostics(self._h, out.ctypes.data_as(_lib.c_double_p)))
+        return out
+
     def diagnostics(self) -> np.ndarray:
         out = np.zeros(3, np.float64)
         check(lib().sph_cuda_diagnostics(self._h, out.ctypes.data_as(_lib.c_double_p)))
@@ -168,11 +194,12 @@ class Simulation:
         return self._probe(lib().sph_cuda_probe_viscosity, params)
 
     def kernel_times(self, params: dict | None = None) -> dict:
-        """Runs ONE step with per-kernel CUDA events; {kernel name: ms}."""
-        t = tunables(params or self.params)
+        """Runs ONE step with per-kernel CUDA events; {kernel name: ms}.
+        params None keeps the tunables of the previous step."""
+        t = None if params is None else ctypes.byref(tunables(params))
         ms = np.zeros(32, np.float32)
         cnt = ctypes.c_int(0)
-        check(lib().sph_cuda_kernel_times(self._h, ctypes.byref(t), _f(ms), 32, ctypes.byref(cnt)))
+        check(lib().sph_cuda_kernel_times(self._h, t, _f(ms), 32, ctypes.byref(cnt)))
         return {lib().sph_cuda_kernel_name(k).decode(): float(ms[k]) for k in range(cnt.value)}
 
     def launches_per_step(self) -> int:
@@ -186,6 +213,42 @@ class Simulation:
         ms = ctypes.c_float(0.0)
         check(lib().sph_cuda_timer_stop(self._h, ctypes.byref(ms)))
         return float(ms.value)
+
+
+class Ensemble(Simulation):
+    """Many independent scenes advanced together by one handle
+    (sph_cuda_create_ensemble): one set of kernel launches per step covers
+    every scene; particles are concatenated in scene order."""
+
+    def __init__(self, scenes: list, max_bucket: int = 100, max_neighbors: int = 400):
+        descs = (_lib.SceneDesc * len(scenes))()
+        for d, sc in zip(descs, scenes):
+            d.params = tunables(sc.params.as_dict())
+            d.boundary.min_x, d.boundary.max_x, d.boundary.min_y, d.boundary.max_y = sc.box
+            d.spacing = sc.spacing
+            d.size_x, d.size_y = sc.size_x, sc.size_y
+            d.n = sc.n
+        self._h = ctypes.c_void_p()
+        check(lib().sph_cuda_create_ensemble(ctypes.byref(self._h), descs, len(scenes),
+                                             int(max_bucket), int(max_neighbors)))
+        self.scenes = scenes
+        self.offsets = np.concatenate([[0], np.cumsum([sc.n for sc in scenes])]).astype(np.int64)
+        self.capacity = int(self.offsets[-1])
+        self.params = None
+        self.config = None
+        self.n = 0
+
+    def upload_scenes(self):
+        cat = lambda k: np.concatenate([getattr(sc, k) for sc in self.scenes])  # noqa: E731
+        self.upload(cat("x"), cat("y"), cat("vx"), cat("vy"))
+
+    def step(self, params=None, nsteps: int = 1):
+        if params is not None:
+            raise ValueError("an ensemble takes per-scene tunables: use set_scene_params")
+        check(lib().sph_cuda_step(self._h, None, int(nsteps)))
+
+    def scene_slice(self, s: int) -> slice:
+        return slice(int(self.offsets[s]), int(self.offsets[s + 1]))
 
 
 class PinnedArray:
