@@ -247,10 +247,12 @@ int sph_cuda_density_static(const float *x, const float *y, int n, const neighbo
 
 /* Runs ONE step (it advances the state) with a CUDA event pair around each
  * kernel on the handle's stream.  ms[k] receives kernel k's time, *count the
- * number of kernels (at most max); names via sph_cuda_kernel_name(k). */
+ * number of kernels (at most max); names via sph_cuda_step_kernel_name(h, k)
+ * (sph_cuda_kernel_name(k) names the kernels of the plain step). */
 int sph_cuda_kernel_times(sph_cuda_t *h, const tunable_parameters *tp, float *ms, int max,
                           int *count);
 const char *sph_cuda_kernel_name(int k);
+const char *sph_cuda_step_kernel_name(sph_cuda_t *h, int k);
 
 /* Kernels launched per step (graph nodes). */
 int sph_cuda_launches_per_step(sph_cuda_t *h);

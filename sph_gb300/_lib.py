@@ -133,6 +133,7 @@ _SIGS = {
     "sph_cuda_kernel_times": (ctypes.c_int, [_P, ctypes.POINTER(TunableParameters), c_float_p,
                                              ctypes.c_int, c_int_p]),
     "sph_cuda_kernel_name": (ctypes.c_char_p, [ctypes.c_int]),
+    "sph_cuda_step_kernel_name": (ctypes.c_char_p, [_P, ctypes.c_int]),
     "sph_cuda_launches_per_step": (ctypes.c_int, [_P]),
     "sph_cuda_timer_start": (ctypes.c_int, [_P]),
     "sph_cuda_timer_stop": (ctypes.c_int, [_P, c_float_p]),
@@ -140,6 +141,24 @@ _SIGS = {
     "sph_cuda_host_free": (ctypes.c_int, [_P]),
     "sph_cuda_last_error": (ctypes.c_char_p, []),
     "sph_cuda_abi_sizes": (ctypes.c_int, [c_int_p, ctypes.c_int]),
+    # learned relaxation (include/sph_learned.h)
+    "sph_learned_create": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_int, ctypes.c_ulonglong]),
+    "sph_learned_destroy": (ctypes.c_int, [_P]),
+    "sph_learned_collect": (ctypes.c_int, [_P, _P, ctypes.c_float, c_int_p]),
+    "sph_learned_num_samples": (ctypes.c_int, [_P]),
+    "sph_learned_clear_samples": (ctypes.c_int, [_P]),
+    "sph_learned_train": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.c_float, c_float_p]),
+    "sph_learned_calibrate": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_float, c_float_p]),
+    "sph_learned_num_params": (ctypes.c_int, []),
+    "sph_learned_get_params": (ctypes.c_int, [_P, c_float_p]),
+    "sph_learned_set_params": (ctypes.c_int, [_P, c_float_p]),
+    "sph_learned_forward": (ctypes.c_int, [_P, c_float_p, ctypes.c_int, c_float_p]),
+    "sph_learned_features": (ctypes.c_int, [_P, c_float_p, c_int_p]),
+    "sph_learned_gemm_check": (ctypes.c_int, [c_float_p, c_float_p, c_float_p, ctypes.c_int,
+                                              ctypes.c_int, ctypes.c_int]),
+    "sph_cuda_set_learned": (ctypes.c_int, [_P, _P, ctypes.c_float]),
+    "sph_cuda_learned_counts": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_ulonglong),
+                                               ctypes.POINTER(ctypes.c_ulonglong)]),
 }
 
 

@@ -181,6 +181,7 @@ static int check_n(sph_cuda *h, int n)
 static void free_all(sph_cuda *h)
 {
     destroy_graph(h);
+    free_learned_buffers(h);
     void *ptrs[] = {h->pos_a, h->vel_a, h->id_a, h->pos_b, h->prev_b, h->vel_b, h->kr_b,
                     h->pos_c, h->prev_c, h->xr_c, h->mask01_c, h->mask2_c, h->id_c,
                     h->tmp_id, h->cnt, h->start_a, h->start_c, h->tile_sums, h->d_scenes,
@@ -832,7 +833,7 @@ int sph_cuda_kernel_times(sph_cuda_t *h, const tunable_parameters *tp, float *ms
     SPH_TRY(apply_tp(h, tp));
     if (h->n == 0) return SPH_OK;
     cudaEvent_t ev[kMaxKernelsPerStep + 1];
-    const int ne = step_kernel_count() + 1;
+    const int ne = step_kernel_count(h) + 1;
     for (int i = 0; i < ne; ++i) SPH_CUDA(cudaEventCreate(&ev[i]));
     int nk = 0;
     int rc = enqueue_step(h, ev, &nk);
@@ -847,10 +848,12 @@ int sph_cuda_kernel_times(sph_cuda_t *h, const tunable_parameters *tp, float *ms
 
 const char *sph_cuda_kernel_name(int k) { return sph::kernel_name(k); }
 
+const char *sph_cuda_step_kernel_name(sph_cuda_t *h, int k) { return sph::step_kernel_name(h, k); }
+
 int sph_cuda_launches_per_step(sph_cuda_t *h)
 {
     if (!h) return 0;
-    return step_kernel_count();
+    return step_kernel_count(h);
 }
 
 int sph_cuda_set_launch_shapes(sph_cuda_t *h, const int *shapes)

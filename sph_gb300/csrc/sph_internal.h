@@ -51,7 +51,10 @@ struct DevState {
     unsigned int list_cap_risk;
     unsigned int lists_valid;      // a neighbour relation exists: viscosity is on
     unsigned int build_max_occ[4]; // per build slot, reset by the build's key producer
-    unsigned int pad[5];
+    unsigned int fb_count;         // learned step: particles on the fallback list
+    unsigned int pad[4];
+    unsigned long long learned_steps;     // steps run with a learned model attached
+    unsigned long long learned_fallback;  // particle-steps of those that used the plain relaxation
 };
 
 enum BuildSlot { SLOT_PREDICTED = 0, SLOT_RELAXED = 1, SLOT_UPLOAD = 2, SLOT_PROBE = 3 };
@@ -72,6 +75,8 @@ struct Shape {
     int block = kBlock;
     int persistent = 0;
 };
+
+struct LearnedModel;
 
 }  // namespace sph
 
@@ -130,6 +135,14 @@ struct sph_cuda {
 
     sph::Shape shape[sph::kGathers];  // launch shapes of the gathers (autotuned)
 
+    // learned relaxation (attached model, its threshold and per-step buffers in C order)
+    sph::LearnedModel *learned = nullptr;
+    float learned_thr = 0.01f;
+    void *feat_c = nullptr;          // BF16 feature rows, 32 per particle
+    unsigned short *nbc_c = nullptr;  // neighbour counts (65535: never use the network)
+    float4 *net_c = nullptr;         // network outputs (dx / s, dy / s, error, 0)
+    int *fb_list = nullptr;          // slots that take the plain relaxation this step
+
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     int graph_n = -1;
@@ -160,6 +173,12 @@ int ensure_stage(sph_cuda *h, size_t bytes);
 int upload_soa_device(sph_cuda *h, int n);  // pos_b/vel_b (id order) + xr_c -> state
 int set_scene_params(sph_cuda *h, int scene, const tunable_parameters *tp);
 int enqueue_step(sph_cuda *h, cudaEvent_t *events, int *nkernels);
+int enqueue_predicted_state(sph_cuda *h);       // first half of a step: C order + density
+int launch_learned_passes(sph_cuda *h, cudaEvent_t *events);  // features + network (C order)
+int launch_learned_relax(sph_cuda *h, float2 *probe_out, cudaEvent_t *events = nullptr);
+void free_learned_buffers(sph_cuda *h);
+const char *step_kernel_name(const sph_cuda *h, int k);
+int step_kernel_count(const sph_cuda *h);
 int run_steps(sph_cuda *h, int nsteps);
 
 }  // namespace sph

@@ -21,9 +21,11 @@
 // atomics are the integer cell-histogram increments, whose arrival rank is
 // used solely to give each particle a distinct scratch slot; the final
 // in-cell order is by id, recomputed deterministically in `permute`.
+#include <algorithm>
 #include <cstdio>
 
 #include "sph_device.cuh"
+#include "sph_learned.h"
 
 namespace sph {
 
@@ -564,13 +566,27 @@ __device__ __forceinline__ void relax_pair(const RelaxConsts &c, float2 p, float
 // Walks the density pass's hit masks; rows longer than kMaskRow (or
 // overflowing buckets) fall back to the whole stencil.
 // PROBE writes the displacement instead of advancing.
-template <bool PROBE>
+// The network's output for a learned step: particle i takes the displacement
+// (net.x, net.y) * s, s = h dt^2 (k + k_near + k_spring), when it has at most
+// max_nb neighbours (counts of 65535 mark particles the network must not
+// take) and the predicted density error net.z (percent of rest density) is
+// at most thr_pct; every other particle runs the plain relaxation.
+struct LearnedIn {
+    const float4 *net = nullptr;
+    const unsigned short *nbc = nullptr;
+    float thr_pct = 0.0f;
+    int max_nb = 0;
+    bool defer = false;  // leave the fallback particles to a second pass
+};
+
+template <bool PROBE, bool LEARNED = false>
 __device__ __forceinline__ void relax_update_one(
     int i, const Ctx &cx, const float4 *__restrict__ xr, const ulonglong2 *__restrict__ mask01,
     const unsigned long long *__restrict__ mask2, const float2 *__restrict__ prev,
     const int *__restrict__ ids, const int *__restrict__ start, bool capped,
     float2 *__restrict__ pos_out, float2 *__restrict__ vel_out, uint2 *__restrict__ kr_out,
-    unsigned *__restrict__ cnt, float2 *__restrict__ probe_out)
+    unsigned *__restrict__ cnt, float2 *__restrict__ probe_out, const LearnedIn &L = LearnedIn(),
+    bool *used_net = nullptr)
 {
     const Scene *S = cx.scenes + scene_of(cx, i);
     const SG g = load_grid(S);
@@ -591,7 +607,19 @@ __device__ __forceinline__ void relax_update_one(
     const unsigned key = cell_key(p.x, p.y, g);
     float ax = 0.0f, ay = 0.0f;
     int nudges = 0;
-    if (searchable(key, i, start, g, capped, cx.max_bucket)) {
+    bool net = false;
+    if (LEARNED && (int)__ldg(L.nbc + i) <= L.max_nb) {
+        const float4 y = __ldg(L.net + i);
+        if (y.z <= L.thr_pct) {
+            const float s = c.hh * c.dt2 * (c.k + c.k_near + 2.0f * c.half_spring);
+            ax = y.x * s;
+            ay = y.y * s;
+            net = true;
+        }
+    }
+    if (LEARNED && used_net) *used_net = net;
+    if (LEARNED && !net && L.defer) return;
+    if (!net && searchable(key, i, start, g, capped, cx.max_bucket)) {
         bool walked = false;
         if (!capped) {
             int ra[3], rl[3];
@@ -661,6 +689,63 @@ k_relax_update(Ctx c, const float4 *__restrict__ xr, const ulonglong2 *__restric
     for (int i = i0; i < c.n; i += gridDim.x * blockDim.x)
         relax_update_one<PROBE>(i, c, xr, mask01, mask2, prev, ids, start, capped, pos_out,
                                 vel_out, kr_out, cnt, probe_out);
+}
+
+// The relaxation pass of a learned step (one particle per thread).  PROBE:
+// every particle's displacement, fallback included.  Otherwise the particles
+// that take the network are advanced here and the others are appended to
+// fb_list (one atomic per warp that has any) for k_relax_fallback, so that
+// the rare plain gathers do not hold up whole warps.  Block 0 counts the step.
+template <bool PROBE>
+__global__ void __launch_bounds__(kBlock, 4)
+k_relax_learned(Ctx c, const float4 *__restrict__ xr, const ulonglong2 *__restrict__ mask01,
+                const unsigned long long *__restrict__ mask2, const float2 *__restrict__ prev,
+                const int *__restrict__ ids, const int *__restrict__ start,
+                const unsigned *__restrict__ occ_in, unsigned *occ_reset,
+                float2 *__restrict__ pos_out, float2 *__restrict__ vel_out,
+                uint2 *__restrict__ kr_out, unsigned *__restrict__ cnt,
+                float2 *__restrict__ probe_out, LearnedIn L, DevState *st, int *__restrict__ fb_list)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (!PROBE && i == 0) {
+        *occ_reset = 0u;
+        atomicAdd(&st->learned_steps, 1ull);
+    }
+    const bool capped = *occ_in > (unsigned)c.max_bucket;
+    bool used = true;
+    L.defer = !PROBE;
+    if (i < c.n)
+        relax_update_one<PROBE, true>(i, c, xr, mask01, mask2, prev, ids, start, capped, pos_out,
+                                      vel_out, kr_out, cnt, probe_out, L, &used);
+    if (PROBE) return;
+    const unsigned fb = __ballot_sync(0xffffffffu, !used);
+    if (fb) {
+        const int lane = threadIdx.x & 31, leader = __ffs(fb) - 1;
+        unsigned base = 0;
+        if (lane == leader) base = atomicAdd(&st->fb_count, (unsigned)__popc(fb));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (!used) fb_list[base + __popc(fb & ((1u << lane) - 1u))] = i;
+    }
+}
+
+// The fallback particles of a learned step: the plain relaxation + update
+// for each slot on fb_list (grid-stride: the count is known on the device
+// only).  Block 0 adds the count to the fallback statistics.
+__global__ void __launch_bounds__(kBlock, 4)
+k_relax_fallback(Ctx c, const float4 *__restrict__ xr, const ulonglong2 *__restrict__ mask01,
+                 const unsigned long long *__restrict__ mask2, const float2 *__restrict__ prev,
+                 const int *__restrict__ ids, const int *__restrict__ start,
+                 const unsigned *__restrict__ occ_in, float2 *__restrict__ pos_out,
+                 float2 *__restrict__ vel_out, uint2 *__restrict__ kr_out,
+                 unsigned *__restrict__ cnt, DevState *st, const int *__restrict__ fb_list)
+{
+    const unsigned total = st->fb_count;
+    const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t0 == 0) atomicAdd(&st->learned_fallback, (unsigned long long)total);
+    const bool capped = *occ_in > (unsigned)c.max_bucket;
+    for (unsigned k = t0; k < total; k += gridDim.x * blockDim.x)
+        relax_update_one<false>(fb_list[k], c, xr, mask01, mask2, prev, ids, start, capped,
+                                pos_out, vel_out, kr_out, cnt, nullptr);
 }
 
 // ---------------------------------------------------------------------------
@@ -892,10 +977,18 @@ static const char *const kKernelNames[] = {
     "cell_permute_1",    "density",            "relax_update",       "cell_scan_reduce_2",
     "cell_scan_apply_2", "cell_scatter_2",     "cell_permute_2"};
 static const int kStepKernels = 11;
+// A step with a learned model: density becomes the feature pass, then the
+// network, then the relaxation with fallback.
+static const char *const kLearnedKernelNames[] = {
+    "viscosity_predict", "cell_scan_reduce_1", "cell_scan_apply_1", "cell_scatter_1",
+    "cell_permute_1",    "features",           "mlp",                "relax_learned",
+    "relax_fallback",    "cell_scan_reduce_2", "cell_scan_apply_2",  "cell_scatter_2",
+    "cell_permute_2"};
+static const int kLearnedStepKernels = 13;
 
-// Queues one step.  With `events` (kStepKernels + 1 of them) each kernel is
-// bracketed for timing.
-int enqueue_step(sph_cuda *h, cudaEvent_t *events, int *nkernels)
+// Viscosity + prediction, the rebuild into the C order (kernels 0-4 of a step).
+template <class Mark>
+static void enqueue_predict_sort(sph_cuda *h, Mark &mark)
 {
     const int n = h->n;
     const int nb = blocks_for(n);
@@ -903,12 +996,6 @@ int enqueue_step(sph_cuda *h, cudaEvent_t *events, int *nkernels)
     const int tiles = (M + kScanTile - 1) / kScanTile;
     const Ctx c = make_ctx(h);
     DevState *st = h->d_state;
-    int e = 0;
-    auto mark = [&]() {
-        if (events) cudaEventRecord(events[e], h->stream);
-        ++e;
-    };
-    mark();
     {
         auto kv = h->shape[0].persistent ? k_viscosity_predict<false, true>
                                          : k_viscosity_predict<false, false>;
@@ -928,21 +1015,99 @@ int enqueue_step(sph_cuda *h, cudaEvent_t *events, int *nkernels)
     k_permute<<<nb, kBlock, 0, h->stream>>>(n, h->kr_b, h->start_c, h->tmp_id, h->id_a, h->pos_b,
                                             h->prev_b, h->id_c, h->pos_c, h->prev_c, nullptr);
     mark();
-    {
-        auto kd = h->shape[1].persistent ? k_density_t<true> : k_density_t<false>;
-        kd<<<gather_grid(h, h->shape[1]), h->shape[1].block, 0, h->stream>>>(
-            c, h->pos_c, h->start_c, &st->build_max_occ[SLOT_PREDICTED], h->xr_c, h->mask01_c,
-            h->mask2_c);
+}
+
+static void enqueue_density(sph_cuda *h)
+{
+    DevState *st = h->d_state;
+    auto kd = h->shape[1].persistent ? k_density_t<true> : k_density_t<false>;
+    kd<<<gather_grid(h, h->shape[1]), h->shape[1].block, 0, h->stream>>>(
+        make_ctx(h), h->pos_c, h->start_c, &st->build_max_occ[SLOT_PREDICTED], h->xr_c,
+        h->mask01_c, h->mask2_c);
+}
+
+// The C-order state of the next step's relaxation -- predicted positions,
+// their cell starts, density records and hit masks -- without advancing:
+// the A state is left as it is (the last step's density record in xr_c is
+// replaced).
+int enqueue_predicted_state(sph_cuda *h)
+{
+    if (h->n == 0) return SPH_OK;
+    auto none = []() {};
+    enqueue_predict_sort(h, none);
+    enqueue_density(h);
+    return cuda_fail(cudaGetLastError(), "predicted state");
+}
+
+// The relaxation passes of a learned step (network particles, then the
+// fallback list); with probe_out, one pass writes every particle's
+// displacement (C order) instead of advancing.  `events` (two) are recorded
+// after each pass.
+int launch_learned_relax(sph_cuda *h, float2 *probe_out, cudaEvent_t *events)
+{
+    const Ctx c = make_ctx(h);
+    DevState *st = h->d_state;
+    LearnedIn L;
+    L.net = h->net_c;
+    L.nbc = h->nbc_c;
+    L.thr_pct = h->learned_thr * 100.0f;
+    // a negative threshold sends every particle to the plain relaxation
+    L.max_nb = h->learned_thr < 0.0f ? -1 : SPH_LEARNED_MAX_NEIGHBORS;
+    const int nb = blocks_for(h->n);
+    const unsigned *occ = &st->build_max_occ[SLOT_PREDICTED];
+    if (probe_out) {
+        k_relax_learned<true><<<nb, kBlock, 0, h->stream>>>(
+            c, h->xr_c, h->mask01_c, h->mask2_c, h->prev_c, h->id_c, h->start_c, occ, nullptr,
+            nullptr, nullptr, nullptr, nullptr, probe_out, L, st, nullptr);
+        return cuda_fail(cudaGetLastError(), "learned relaxation probe");
     }
+    k_relax_learned<false><<<nb, kBlock, 0, h->stream>>>(
+        c, h->xr_c, h->mask01_c, h->mask2_c, h->prev_c, h->id_c, h->start_c, occ,
+        &st->build_max_occ[SLOT_RELAXED], h->pos_b, h->vel_b, h->kr_b, h->cnt, nullptr, L, st,
+        h->fb_list);
+    if (events) cudaEventRecord(events[0], h->stream);
+    const int fb_blocks = std::min(nb, 4 * h->num_sms);
+    k_relax_fallback<<<fb_blocks, kBlock, 0, h->stream>>>(
+        c, h->xr_c, h->mask01_c, h->mask2_c, h->prev_c, h->id_c, h->start_c, occ, h->pos_b,
+        h->vel_b, h->kr_b, h->cnt, st, h->fb_list);
+    if (events) cudaEventRecord(events[1], h->stream);
+    return cuda_fail(cudaGetLastError(), "learned relaxation");
+}
+
+// Queues one step.  With `events` (one per kernel + 1) each kernel is
+// bracketed for timing.
+int enqueue_step(sph_cuda *h, cudaEvent_t *events, int *nkernels)
+{
+    const int n = h->n;
+    const int nb = blocks_for(n);
+    const int M = h->M;
+    const int tiles = (M + kScanTile - 1) / kScanTile;
+    const Ctx c = make_ctx(h);
+    DevState *st = h->d_state;
+    int e = 0;
+    auto mark = [&]() {
+        if (events) cudaEventRecord(events[e], h->stream);
+        ++e;
+    };
     mark();
-    {
+    enqueue_predict_sort(h, mark);
+    if (h->learned) {
+        int rc = launch_learned_passes(h, events ? events + e : nullptr);
+        if (rc != SPH_OK) return rc;
+        e += 2;
+        rc = launch_learned_relax(h, nullptr, events ? events + e : nullptr);
+        if (rc != SPH_OK) return rc;
+        e += 2;
+    } else {
+        enqueue_density(h);
+        mark();
         auto kr = h->shape[2].persistent ? k_relax_update<false, true> : k_relax_update<false, false>;
         kr<<<gather_grid(h, h->shape[2]), h->shape[2].block, 0, h->stream>>>(
             c, h->xr_c, h->mask01_c, h->mask2_c, h->prev_c, h->id_c, h->start_c,
             &st->build_max_occ[SLOT_PREDICTED], &st->build_max_occ[SLOT_RELAXED], h->pos_b,
             h->vel_b, h->kr_b, h->cnt, nullptr);
+        mark();
     }
-    mark();
     k_scan_reduce<<<tiles, kScanThreads, 0, h->stream>>>(h->cnt, M, h->d_nocell, h->tile_sums, st,
                                                          &st->build_max_occ[SLOT_RELAXED],
                                                          h->max_bucket, h->max_neighbors);
@@ -962,7 +1127,16 @@ const char *kernel_name(int k)
 {
     return (k >= 0 && k < kStepKernels) ? kKernelNames[k] : "";
 }
+const char *step_kernel_name(const sph_cuda *h, int k)
+{
+    if (h && h->learned) return (k >= 0 && k < kLearnedStepKernels) ? kLearnedKernelNames[k] : "";
+    return kernel_name(k);
+}
 int step_kernel_count() { return kStepKernels; }
+int step_kernel_count(const sph_cuda *h)
+{
+    return (h && h->learned) ? kLearnedStepKernels : kStepKernels;
+}
 
 // Upload tail: pos_b / vel_b (id order) -> sorted A state; prev_c / xr_c
 // already hold the uploaded values in id order.

@@ -225,6 +225,24 @@ def config3(nscenes: int = 512, n_range=(1024, 65536)) -> list:
     return out
 
 
+def learned_training_scenes(count: int = 200, n: int = 65_536, seed0: int = 4000) -> list:
+    """Training trajectories of the learned relaxation: `count` dam breaks of
+    config 2's construction at `n` particles (mover held at its t = 0
+    position), each with k ~ U[0.1, 0.5], k_near ~ U[1, 3], sigma ~ U[0, 1]
+    drawn from counters 0..2 of seed seed0 + s (the ensemble's ranges)."""
+    out = []
+    for s in range(count):
+        sc = config2(n)
+        u = uniform(seed0 + s, np.arange(3, dtype=np.uint64))
+        sc.params.k = float(0.1 + 0.4 * u[0])
+        sc.params.k_near = float(1.0 + 2.0 * u[1])
+        sc.params.sigma = float(u[2])
+        sc.mover_period = 0.0
+        sc.name = f"learned_train_{s}"
+        out.append(sc)
+    return out
+
+
 def algorithmic_bytes_per_step(n: int, cells: int) -> int:
     """Canonical algorithmic HBM bytes of one step: 216 B per particle
     (viscosity+predict 40, cell build on predicted positions 68, density 16,

@@ -200,7 +200,8 @@ class Simulation:
         ms = np.zeros(32, np.float32)
         cnt = ctypes.c_int(0)
         check(lib().sph_cuda_kernel_times(self._h, t, _f(ms), 32, ctypes.byref(cnt)))
-        return {lib().sph_cuda_kernel_name(k).decode(): float(ms[k]) for k in range(cnt.value)}
+        return {lib().sph_cuda_step_kernel_name(self._h, k).decode(): float(ms[k])
+                for k in range(cnt.value)}
 
     def launches_per_step(self) -> int:
         return int(lib().sph_cuda_launches_per_step(self._h))
@@ -213,6 +214,130 @@ class Simulation:
         ms = ctypes.c_float(0.0)
         check(lib().sph_cuda_timer_stop(self._h, ctypes.byref(ms)))
         return float(ms.value)
+
+
+    # -- learned relaxation -------------------------------------------------
+    def set_learned(self, model: "LearnedModel | None", threshold: float = 0.01):
+        """Attaches a trained model (None detaches): particles whose
+        predicted density error is at most `threshold` x rest density take
+        the network's displacement, the rest the plain relaxation."""
+        check(lib().sph_cuda_set_learned(self._h, None if model is None else model._l,
+                                         float(threshold)))
+        self._learned = model
+
+    def learned_counts(self) -> tuple:
+        """(particle-steps that used the network, particle-steps that fell
+        back) since the model was attached."""
+        a, b = ctypes.c_ulonglong(0), ctypes.c_ulonglong(0)
+        check(lib().sph_cuda_learned_counts(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return int(a.value), int(b.value)
+
+    def learned_features(self):
+        """(features [n, 32] float32 by id, neighbour counts [n] int32, -1
+        for particles that always take the plain relaxation) of the state
+        the next step relaxes."""
+        f = np.zeros((self.n, LearnedModel.IN), np.float32)
+        c = np.zeros(self.n, np.int32)
+        check(lib().sph_learned_features(self._h, _f(f), c.ctypes.data_as(_lib.c_int_p)))
+        return f, c
+
+
+class LearnedModel:
+    """The learned relaxation's network (include/sph_learned.h): a 2-layer,
+    width-128 GELU MLP over per-particle neighbour messages, BF16 on the
+    tcgen05 tensor cores with FP32 accumulation and FP32 Adam."""
+
+    IN, HIDDEN, OUT, MAX_NEIGHBORS = 32, 128, 16, 48
+
+    def __init__(self, max_samples: int, seed: int = 0):
+        self._l = ctypes.c_void_p()
+        check(lib().sph_learned_create(ctypes.byref(self._l), int(max_samples), int(seed)))
+
+    def close(self):
+        if self._l is not None and self._l.value:
+            check(lib().sph_learned_destroy(self._l))
+        self._l = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @staticmethod
+    def num_params() -> int:
+        return int(lib().sph_learned_num_params())
+
+    def collect(self, sim: Simulation, fraction: float = 1.0) -> int:
+        n = ctypes.c_int(0)
+        check(lib().sph_learned_collect(self._l, sim.handle, float(fraction), ctypes.byref(n)))
+        return int(n.value)
+
+    @property
+    def num_samples(self) -> int:
+        return int(lib().sph_learned_num_samples(self._l))
+
+    def clear_samples(self):
+        check(lib().sph_learned_clear_samples(self._l))
+
+    def train(self, epochs: int, batch: int = 4096, lr: float = 1e-3) -> float:
+        loss = ctypes.c_float(0.0)
+        check(lib().sph_learned_train(self._l, int(epochs), int(batch), float(lr), ctypes.byref(loss)))
+        return float(loss.value)
+
+    def calibrate(self, sim: Simulation, epochs: int = 4, lr: float = 1e-3) -> float:
+        loss = ctypes.c_float(0.0)
+        check(lib().sph_learned_calibrate(self._l, sim.handle, int(epochs), float(lr),
+                                          ctypes.byref(loss)))
+        return float(loss.value)
+
+    def get_params(self) -> np.ndarray:
+        w = np.zeros(self.num_params(), np.float32)
+        check(lib().sph_learned_get_params(self._l, _f(w)))
+        return w
+
+    def set_params(self, w: np.ndarray):
+        w = np.ascontiguousarray(w, np.float32)
+        if w.shape != (self.num_params(),):
+            raise ValueError(f"expected {self.num_params()} parameters, got {w.shape}")
+        check(lib().sph_learned_set_params(self._l, _f(w)))
+
+    def forward(self, features: np.ndarray) -> np.ndarray:
+        x = np.ascontiguousarray(features, np.float32)
+        n = x.shape[0]
+        out = np.zeros((n, self.OUT), np.float32)
+        check(lib().sph_learned_forward(self._l, _f(x), n, _f(out)))
+        return out
+
+    @staticmethod
+    def unpack(w: np.ndarray) -> dict:
+        """Named views of a flat parameter vector."""
+        I, H, O = LearnedModel.IN, LearnedModel.HIDDEN, LearnedModel.OUT
+        sizes = [("W1", (H, I)), ("b1", (H,)), ("W2", (H, H)), ("b2", (H,)), ("W3", (O, H)),
+                 ("b3", (O,))]
+        out, o = {}, 0
+        for name, shp in sizes:
+            k = int(np.prod(shp))
+            out[name] = w[o:o + k].reshape(shp)
+            o += k
+        return out
+
+
+def gemm_check(A: np.ndarray, B: np.ndarray) -> np.ndarray:
+    """A [M, K] . B [N, K]^T on the tcgen05 tensor cores (BF16 in, FP32 out)."""
+    A = np.ascontiguousarray(A, np.float32)
+    B = np.ascontiguousarray(B, np.float32)
+    M, K = A.shape
+    N = B.shape[0]
+    C = np.zeros((M, N), np.float32)
+    check(lib().sph_learned_gemm_check(_f(A), _f(B), _f(C), M, N, K))
+    return C
 
 
 class Ensemble(Simulation):
