@@ -17,6 +17,13 @@ dam break), each step with its own mover position.
           against the measured HBM copy bandwidth.
   cpu_baseline  the oracle's restatement of the reference step (Gauss-Seidel,
           single thread) on a bounded sample of the same construction.
+  learned the learned-relaxation step on the same scene: a network trained
+          (in the same run, untimed) on 200 plain-method trajectories of
+          65,536-particle dam breaks with randomised stiffness and viscosity,
+          run with the plain relaxation as fallback where its predicted
+          density error exceeds 1% of the rest density; its throughput, its
+          RMS density error against the plain step, and the tensor-core
+          roofline of its MLP kernel.
 
 --impl reference runs the reference's CPU step instead (the compiled
 reference where present, else the restatement) on all host cores.
@@ -57,6 +64,10 @@ ALG_BYTES = {
 }
 
 
+# MMA work of one network row: 32 -> 128 -> 128 -> 16 (multiply-adds x 2).
+MLP_FLOPS_PER_ROW = 2 * (32 * 128 + 128 * 128 + 128 * 16)
+
+
 def load_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -65,6 +76,16 @@ def load_peaks():
         return float(d["hbm_gbs"]), "measured"
     except Exception:
         return 6800.0, "fallback"
+
+
+def load_tensor_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["bf16_tflops"]), "measured (burst)"
+    except Exception:
+        return 1900.0, "fallback"
 
 
 class ClockSampler:
@@ -331,6 +352,202 @@ class EnsembleWork:
                           f"after one untimed step, reference step order, single thread"}
 
 
+def train_learned(args):
+    """Trains the learned relaxation on plain-method trajectories: one
+    batched ensemble of `train_scenes` dam breaks of `train_n` particles
+    (randomised k, k_near, sigma), sampled every 10 steps; then calibrates
+    its density-error output on one more trajectory's state."""
+    from sph_gb300 import Ensemble, LearnedModel, Simulation, scenes
+    t0 = time.perf_counter()
+    tr = scenes.learned_training_scenes(args.train_scenes, args.train_n)
+    total = sum(s.n for s in tr)
+    every, steps = 10, args.train_steps
+    frac = min(1.0, args.train_samples / (total * (steps // every)))
+    m = LearnedModel(int(args.train_samples * 1.1) + 2 * args.train_n, seed=20261)
+    e = Ensemble(tr)
+    e.upload_scenes()
+    for t in range(0, steps, every):
+        e.step(None, every)
+        m.collect(e, frac)
+    e.close()
+    t_collect = time.perf_counter() - t0
+    losses = []
+    for ep in range(args.train_epochs):
+        lr = 1e-3 if ep < args.train_epochs - 2 else 3e-4
+        losses.append(m.train(1, 4096, lr))
+    cal_sc = scenes.learned_training_scenes(1, args.train_n, seed0=4000 + args.train_scenes)[0]
+    with Simulation.from_scene(cal_sc) as s:
+        s.step(cal_sc.params.as_dict(), 200)
+        cal_loss = m.calibrate(s, epochs=4)
+    info = {"trajectories": len(tr), "particles_per_trajectory": args.train_n,
+            "steps_per_trajectory": steps, "samples": m.num_samples, "sample_every": every,
+            "epochs": args.train_epochs, "loss_per_epoch": [round(v, 6) for v in losses],
+            "calibration_loss": cal_loss, "collect_s": t_collect,
+            "train_s": time.perf_counter() - t0 - t_collect}
+    m.clear_samples()
+    return m, info
+
+
+def run_learned(args, work, plain_ms):
+    """The learned step on the dam break: throughput (CUDA events around
+    graph-launched steps), one-step RMS density error against the plain step
+    from the same state, the fallback share, and a 1,000-step trajectory's
+    mean density and kinetic energy against the plain method's."""
+    import numpy as np
+    model, info = train_learned(args)
+    thr = args.learned_threshold
+    K, W = args.steps, args.warmup
+    sim = work.fresh()
+    work.advance(sim, 0, W)
+    sim.set_learned(model, thr)
+    work.advance(sim, W, 5)
+    sim.synchronize()
+    with ClockSampler(0) as clk:
+        sim.timer_start()
+        work.advance(sim, W + 5, K)
+        ms = sim.timer_stop()
+    clocks = clk.summary()
+    used, fell = sim.learned_counts()
+    kt_runs = [sim.kernel_times(None) for _ in range(5)]
+    ktimes = {k: statistics.median(r[k] for r in kt_runs) for k in kt_runs[0]}
+    sim.close()
+    n = work.n
+    peak, peak_kind = load_tensor_peak()
+    flops = MLP_FLOPS_PER_ROW * n
+    achieved = flops / (ktimes["mlp"] / 1e3) / 1e12
+
+    # one-step density error against the plain step from the same state
+    t_state = 200
+    a, b = work.fresh(), work.fresh()
+    work.advance(a, 0, t_state)
+    work.advance(b, 0, t_state)
+    b.set_learned(model, thr)
+    work.step_one(a, t_state)
+    work.step_one(b, t_state)
+    pa = work.p(t_state + 1)
+    ra, _ = a.probe_density(pa)
+    rb, _ = b.probe_density(pa)
+    rest = work.sc.params.rest_density
+    rms = float(np.sqrt(np.mean((ra.astype(np.float64) - rb) ** 2)) / rest)
+    u1, f1 = b.learned_counts()
+    # trajectories: plain vs learned over the scene's 1,000 steps
+    traj = None
+    if not args.no_trajectory:
+        steps = work.sc.steps - t_state - 1
+        work.advance(a, t_state + 1, steps)
+        work.advance(b, t_state + 1, steps)
+        da, db = a.diagnostics(), b.diagnostics()
+        traj = {"steps": work.sc.steps, "plain": {"mean_density": da[0], "kinetic_energy": da[2]},
+                "learned": {"mean_density": db[0], "kinetic_energy": db[2]},
+                "mean_density_rel_diff": abs(db[0] - da[0]) / da[0],
+                "kinetic_energy_rel_diff": abs(db[2] - da[2]) / max(abs(da[2]), 1e-30)}
+    a.close()
+    b.close()
+    model.close()
+    return {"value": n * K / (ms / 1e3), "unit": "particle-steps/s", "ms_per_step": ms / K,
+            "vs_plain": (plain_ms) / (ms / K), "threshold_rest_density": thr,
+            "network_share": used / max(1, used + fell),
+            "rms_density_error_one_step": rms, "one_step_network_share": u1 / max(1, u1 + f1),
+            "trajectory": traj, "training": info, "clocks": clocks,
+            "roofline": {"bound": "tensor", "kernel": "mlp", "achieved": achieved, "peak": peak,
+                         "unit": "TFLOP/s", "frac": achieved / peak, "peak_source": peak_kind,
+                         "flops_per_launch": flops},
+            "kernel_ms": {k: round(v, 5) for k, v in ktimes.items()}}
+
+
+def run_skewed(args, world, rank):
+    """Learned relaxation + batching under skew: 2,048 scenes (settled piles
+    with Gaussian blobs dropped on them) in one graph-captured step with the
+    learned relaxation, against the same ensemble with the plain step."""
+    import numpy as np
+
+    from sph_gb300 import Ensemble, scenes
+    piles = scenes.config5(args.scenes)
+    t0 = time.perf_counter()
+    scs = scenes.settle_and_drop(piles, scenes.SETTLE_STEPS)
+    t_settle = time.perf_counter() - t0
+    n = sum(s.n for s in scs)
+    cells = sum(s.cells for s in scs)
+    model, info = train_learned(args)
+    K, W = args.steps, args.warmup
+
+    def fresh(learned):
+        e = Ensemble(scs)
+        e.upload_scenes()
+        if learned:
+            e.set_learned(model, args.learned_threshold)
+        return e
+
+    res = {}
+    for label in ("plain", "learned"):
+        e = fresh(label == "learned")
+        e.step(None, W)
+        shapes = e.autotune(2)
+        e.synchronize()
+        barrier(world)
+        with ClockSampler(0) as clk:
+            e.timer_start()
+            e.step(None, K)
+            ms = e.timer_stop()
+        ms = max_over_ranks(world, ms)
+        kt = [e.kernel_times(None) for _ in range(3)]
+        res[label] = {"ms": ms, "clocks": clk.summary(), "shapes": shapes,
+                      "launches": e.launches_per_step() * K,
+                      "kernel_ms": {k: round(statistics.median(r[k] for r in kt), 5) for k in kt[0]},
+                      "counts": e.learned_counts() if label == "learned" else None}
+        e.close()
+    # one-step density error against the plain step from the same state
+    a, b = fresh(False), fresh(False)
+    a.step(None, 100)
+    b.step(None, 100)
+    b.set_learned(model, args.learned_threshold)
+    a.step(None, 1)
+    b.step(None, 1)
+    used, fell = b.learned_counts()
+    # densities of the post-step positions (the ensemble's own tunables)
+    da, _ = a.probe_density()
+    db, _ = b.probe_density()
+    rest = scs[0].params.rest_density
+    rms = float(np.sqrt(np.mean((da.astype(np.float64) - db) ** 2)) / rest)
+    a.close()
+    b.close()
+    model.close()
+    L, P = res["learned"], res["plain"]
+    value = world * n * K / (L["ms"] / 1e3)
+    peak, peak_kind = load_tensor_peak()
+    mlp_ms = L["kernel_ms"]["mlp"]
+    achieved = MLP_FLOPS_PER_ROW * n / (mlp_ms / 1e3) / 1e12
+    if rank == 0:
+        occ = []
+        for sc in scs[:256]:
+            k = np.floor(sc.y).astype(np.int64) * sc.size_x + np.floor(sc.x).astype(np.int64)
+            occ.append(int(np.bincount(k).max()))
+        line = {"metric": "particle-steps/s", "value": value, "unit": "particle-steps/s",
+                "n_gpus": world, "steps": K, "warmup": W, "ms_per_step": L["ms"] / K,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32 state, bf16 network", "data": "synthetic",
+                "config": {"workload": f"skewed ensemble, {len(scs)} scenes, {n} particles "
+                                       f"(512-32,768 per scene, log-uniform), settled piles "
+                                       f"({scenes.SETTLE_STEPS} plain steps) + 1-6 Gaussian blobs, "
+                                       f"learned relaxation",
+                           "particles": n, "cells": cells, "settle_s": t_settle,
+                           "max_cell_occupancy_first_256": max(occ),
+                           "parallelism": f"replicas x{world}", "launch_shapes": L["shapes"]},
+                "plain": {"value": world * n * K / (P["ms"] / 1e3), "ms_per_step": P["ms"] / K,
+                          "kernel_ms": P["kernel_ms"], "clocks": P["clocks"]},
+                "learned_vs_plain": P["ms"] / L["ms"],
+                "rms_density_error_one_step": rms,
+                "network_share_one_step": used / max(1, used + fell),
+                "network_share_timed": (L["counts"][0] / max(1, sum(L["counts"]))),
+                "threshold_rest_density": args.learned_threshold,
+                "roofline": {"bound": "tensor", "kernel": "mlp", "achieved": achieved, "peak": peak,
+                             "unit": "TFLOP/s", "frac": achieved / peak, "peak_source": peak_kind,
+                             "flops_per_launch": MLP_FLOPS_PER_ROW * n},
+                "kernel_ms": L["kernel_ms"], "clocks": L["clocks"], "gpu_launches": L["launches"],
+                "training": info, "e2e": None, "cpu_baseline": None}
+        print(json.dumps(line), flush=True)
+
+
 def run_gpu(args, world, rank):
     import numpy as np
 
@@ -399,6 +616,13 @@ def run_gpu(args, world, rank):
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = work.cpu_sample(args)
 
+    learned = None
+    if args.workload == "dam_break" and not args.no_learned:
+        try:
+            learned = run_learned(args, work, ms / K)
+        except Exception as exc:  # reported, never hidden
+            learned = {"error": f"{type(exc).__name__}: {exc}"}
+
     if rank == 0:
         line = {"metric": "particle-steps/s", "value": value, "unit": "particle-steps/s",
                 "n_gpus": world, "steps": K, "warmup": W, "ms_per_step": ms / K,
@@ -409,7 +633,7 @@ def run_gpu(args, world, rank):
                            "l2": "no flush: per-step working set ~0.5 GB > 129 MB L2",
                            "steps_timed": f"{t0}..{t0 + K - 1}", "launch_shapes": shapes},
                 "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
-                "clocks": clocks, "gpu_launches": launches,
+                "clocks": clocks, "gpu_launches": launches, "learned": learned,
                 "diagnostics": {"mean_density": diag[0], "mean_near_density": diag[1],
                                 "kinetic_energy_per_particle": diag[2]},
                 "counters": counters}
@@ -423,17 +647,29 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=4_194_304)
-    ap.add_argument("--workload", default="dam_break", choices=["dam_break", "ensemble"])
+    ap.add_argument("--workload", default="dam_break", choices=["dam_break", "ensemble", "skewed"])
     ap.add_argument("--scenes", type=int, default=512)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=262_144)
     ap.add_argument("--cpu-steps", type=int, default=12)
+    ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--no-trajectory", action="store_true")
+    ap.add_argument("--learned-threshold", type=float, default=0.01)
+    ap.add_argument("--train-scenes", type=int, default=200)
+    ap.add_argument("--train-n", type=int, default=65_536)
+    ap.add_argument("--train-steps", type=int, default=300)
+    ap.add_argument("--train-samples", type=int, default=6_000_000)
+    ap.add_argument("--train-epochs", type=int, default=5)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, _ = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)
+    elif args.workload == "skewed":
+        if args.scenes == 512:
+            args.scenes = 2048
+        run_skewed(args, world, rank)
     else:
         run_gpu(args, world, rank)
     if world > 1:

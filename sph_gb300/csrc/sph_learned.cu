@@ -12,6 +12,7 @@
 // Training: a generic tcgen05 GEMM (strided BF16 operands staged in shared
 // memory, FP32 accumulation), bias/GELU kernels, Adam on FP32 master weights.
 #include <algorithm>
+#include <cstddef>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -44,12 +45,13 @@ constexpr int NPARAM = OFF_B3 + OUT;
 
 // Outputs used: 0, 1 displacement / s; 2 predicted density error in % of rho0.
 
-__device__ __forceinline__ float gelu_grad(float x)
+// Derivative of the activation 2 GELU (tanh form).
+__device__ __forceinline__ float act_grad(float x)
 {
     float t;
     const float u = 0.7978845608f * (x + 0.044715f * x * x * x);
     asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(u));
-    return 0.5f * (1.0f + t) + 0.5f * x * (1.0f - t * t) * 0.7978845608f * (1.0f + 0.134145f * x * x);
+    return (1.0f + t) + x * (1.0f - t * t) * 0.7978845608f * (1.0f + 0.134145f * x * x);
 }
 
 // Output scale of a scene: s = h dt^2 (k + k_near + k_spring).
@@ -207,7 +209,8 @@ k_features(Ctx c, const float2 *__restrict__ pos, const float2 *__restrict__ pre
     f[21] = as * V1x * 0.5f;
     f[22] = as * V1y * 0.5f;
 #pragma unroll
-    for (int e = 23; e < IN; ++e) f[e] = 0.0f;
+    for (int e = 23; e < IN - 1; ++e) f[e] = 0.0f;
+    f[IN - 1] = 1.0f;  // constant input: the first layer's bias
     uint4 *row = reinterpret_cast<uint4 *>(feat + (size_t)i * IN);
 #pragma unroll
     for (int q = 0; q < IN / 8; ++q) {
@@ -224,82 +227,112 @@ k_features(Ctx c, const float2 *__restrict__ pos, const float2 *__restrict__ pre
 // fused MLP inference (tcgen05)
 // ---------------------------------------------------------------------------
 
-struct MlpSmem {
-    // K-major no-swizzle operand tiles
-    unsigned char w1[HID * IN * 2];
-    unsigned char w2[HID * HID * 2];
-    unsigned char w3[OUT * HID * 2];
-    unsigned char x[128 * IN * 2];
-    unsigned char hbuf[128 * HID * 2];
-    float b1[HID], b2[HID], b3[OUT];
-    uint64_t mbar;
+// Inference layout.  The first layer's bias is folded into the weight of
+// the constant feature 31 (= 1); the second layer's bias enters as one more
+// K = 16 MMA of a ones column against the bias column; the activation is
+// 2 GELU (the factor 2 is absorbed by the weights that follow it, in
+// training and inference alike).
+struct alignas(128) MlpWeights {
+    unsigned char w1[HID * IN * 2];    // W1, column 31 + b1
+    unsigned char w2[HID * HID * 2];   // W2
+    unsigned char w2b[HID * 16 * 2];   // column 0 = b2 (BF16), the rest 0
+    unsigned char w3[OUT * HID * 2];   // W3
+    unsigned char ones[128 * 16 * 2];  // column 0 = 1, the rest 0
+    float b3[OUT];
     uint32_t taddr;
 };
 
-// Two CTAs of 256 threads per SM: 2 x 256 TMEM columns, 2 x ~85 KB of
-// shared memory.  One CTA's tensor-core work overlaps the other's epilogue.
-constexpr int kMlpThreads = 256;
-constexpr int kMlpCtasPerSm = 2;
-constexpr uint32_t kTmemCols = 256;  // layer 1 -> [0,128), layer 2 -> [128,256), layer 3 -> [0,16)
+struct alignas(128) MlpPipe {
+    unsigned char x[128 * IN * 2];
+    unsigned char hbuf[128 * HID * 2];
+    uint64_t mbar;
+};
 
-__device__ __forceinline__ void stage_weights(MlpSmem &s, const __nv_bfloat16 *__restrict__ w,
-                                              const float *__restrict__ bias)
+// One CTA per SM of four independent pipelines of 256 threads (8 warps);
+// pipeline p owns TMEM columns [128 p, 128 p + 128) (all three layers of a
+// tile accumulate there in turn), its own operand tiles, mbarrier and named
+// barrier.  The pipelines share the weights; their tensor-core work and
+// epilogues interleave.
+constexpr int kPipes = 4;
+constexpr int kPipeThreads = 256;
+constexpr int kMlpThreads = kPipes * kPipeThreads;
+constexpr uint32_t kTmemCols = 128 * kPipes;
+
+struct MlpSmem {
+    MlpWeights w;
+    MlpPipe pipe[kPipes];
+};
+// operand tiles start on 128-byte boundaries (descriptors and 16-byte stores)
+static_assert(offsetof(MlpWeights, w2) % 128 == 0 && offsetof(MlpWeights, w2b) % 128 == 0 &&
+                  offsetof(MlpWeights, w3) % 128 == 0 && offsetof(MlpWeights, ones) % 128 == 0,
+              "weight tiles aligned");
+static_assert(offsetof(MlpSmem, pipe) % 128 == 0 && sizeof(MlpPipe) % 128 == 0 &&
+                  offsetof(MlpPipe, hbuf) % 128 == 0,
+              "pipeline tiles aligned");
+static_assert(sizeof(MlpSmem) + 1024 <= 227 * 1024, "fits the shared memory of one CTA");
+
+__device__ __forceinline__ void stage_weights(MlpWeights &s, const __nv_bfloat16 *__restrict__ w,
+                                              const float *__restrict__ wf)
 {
     const int t = threadIdx.x;
     for (int e = t; e < HID * IN; e += blockDim.x) {
         const int r = e / IN, k = e % IN;
-        *reinterpret_cast<__nv_bfloat16 *>(s.w1 + tc::kmajor_offset(r, k, IN)) = w[OFF_W1 + e];
+        const __nv_bfloat16 v =
+            k == IN - 1 ? __float2bfloat16(wf[OFF_W1 + e] + wf[OFF_B1 + r]) : w[OFF_W1 + e];
+        *reinterpret_cast<__nv_bfloat16 *>(s.w1 + tc::kmajor_offset(r, k, IN)) = v;
     }
     for (int e = t; e < HID * HID; e += blockDim.x) {
         const int r = e / HID, k = e % HID;
         *reinterpret_cast<__nv_bfloat16 *>(s.w2 + tc::kmajor_offset(r, k, HID)) = w[OFF_W2 + e];
     }
+    for (int e = t; e < HID * 16; e += blockDim.x) {
+        const int r = e / 16, k = e % 16;
+        *reinterpret_cast<__nv_bfloat16 *>(s.w2b + tc::kmajor_offset(r, k, 16)) =
+            __float2bfloat16(k == 0 ? wf[OFF_B2 + r] : 0.0f);
+        *reinterpret_cast<__nv_bfloat16 *>(s.ones + tc::kmajor_offset(r, k, 16)) =
+            __float2bfloat16(k == 0 ? 1.0f : 0.0f);
+    }
     for (int e = t; e < OUT * HID; e += blockDim.x) {
         const int r = e / HID, k = e % HID;
         *reinterpret_cast<__nv_bfloat16 *>(s.w3 + tc::kmajor_offset(r, k, HID)) = w[OFF_W3 + e];
     }
-    for (int e = t; e < HID; e += blockDim.x) {
-        s.b1[e] = bias[OFF_B1 + e];
-        s.b2[e] = bias[OFF_B2 + e];
-    }
-    for (int e = t; e < OUT; e += blockDim.x) s.b3[e] = bias[OFF_B3 + e];
+    for (int e = t; e < OUT; e += blockDim.x) s.b3[e] = wf[OFF_B3 + e];
 }
 
-// Epilogue of a width-128 hidden layer: warp w takes TMEM lanes
-// 32 (w % 4) .. + 31 (one row per thread) and columns col0 + 64 (w / 4) .. + 63;
-// + bias, GELU, BF16 into the K-major activation tile (16-byte stores).
-__device__ __forceinline__ void hidden_epilogue(MlpSmem &s, uint32_t tbase, uint32_t col0,
-                                                const float *bias)
+// Epilogue of a hidden layer in a pipeline: warp w (0..7 within it) takes
+// TMEM lanes 32 (w % 4) .. + 31 (one row per thread) and columns
+// 64 (w / 4) .. + 63 of the pipeline's accumulator; activation in BF16 into
+// the K-major activation tile (16-byte stores).
+__device__ __forceinline__ void hidden_epilogue(unsigned char *hbuf, uint32_t tacc, int tp)
 {
-    const int t = threadIdx.x, w = t >> 5;
-    const int row = 32 * (w & 3) + (t & 31);
+    const int w = tp >> 5;
+    const int row = 32 * (w & 3) + (tp & 31);
     const int c0 = 64 * (w >> 2);
     const uint32_t lane = (uint32_t)(32 * (w & 3)) << 16;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
         const int c = c0 + 32 * h;
         float v[32];
-        tc::tmem_ld32(tbase + lane + col0 + (uint32_t)c, v);
+        tc::tmem_ld32(tacc + lane + (uint32_t)c, v);
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             uint4 o;
-            const float *bq = bias + c + 8 * q;
-            o.x = tc::gelu_bf16x2(v[8 * q + 0] + bq[0], v[8 * q + 1] + bq[1]);
-            o.y = tc::gelu_bf16x2(v[8 * q + 2] + bq[2], v[8 * q + 3] + bq[3]);
-            o.z = tc::gelu_bf16x2(v[8 * q + 4] + bq[4], v[8 * q + 5] + bq[5]);
-            o.w = tc::gelu_bf16x2(v[8 * q + 6] + bq[6], v[8 * q + 7] + bq[7]);
-            *reinterpret_cast<uint4 *>(s.hbuf + tc::kmajor_offset(row, c + 8 * q, HID)) = o;
+            o.x = tc::act_bf16x2(v[8 * q + 0], v[8 * q + 1]);
+            o.y = tc::act_bf16x2(v[8 * q + 2], v[8 * q + 3]);
+            o.z = tc::act_bf16x2(v[8 * q + 4], v[8 * q + 5]);
+            o.w = tc::act_bf16x2(v[8 * q + 6], v[8 * q + 7]);
+            *reinterpret_cast<uint4 *>(hbuf + tc::kmajor_offset(row, c + 8 * q, HID)) = o;
         }
     }
 }
 
-// Half a feature row (16 BF16 = 32 bytes) of row tile*128 + (t >> 1).
+// Half a feature row (16 BF16 = 32 bytes) of row tile*128 + (tp >> 1).
 __device__ __forceinline__ void load_feat(const __nv_bfloat16 *__restrict__ feat, int n, int tile,
-                                          uint4 &a, uint4 &b)
+                                          int tp, uint4 &a, uint4 &b)
 {
-    const int gi = tile * 128 + (threadIdx.x >> 1);
+    const int gi = tile * 128 + (tp >> 1);
     if (gi < n) {
-        const uint4 *src = reinterpret_cast<const uint4 *>(feat + (size_t)gi * IN) + 2 * (threadIdx.x & 1);
+        const uint4 *src = reinterpret_cast<const uint4 *>(feat + (size_t)gi * IN) + 2 * (tp & 1);
         a = __ldcs(src);
         b = __ldcs(src + 1);
     } else {
@@ -308,104 +341,112 @@ __device__ __forceinline__ void load_feat(const __nv_bfloat16 *__restrict__ feat
     }
 }
 
-__device__ __forceinline__ void store_feat(MlpSmem &s, const uint4 &a, const uint4 &b)
+__device__ __forceinline__ void store_feat(unsigned char *x, int tp, const uint4 &a, const uint4 &b)
 {
-    const int r = threadIdx.x >> 1, k = 16 * (threadIdx.x & 1);
-    *reinterpret_cast<uint4 *>(s.x + tc::kmajor_offset(r, k, IN)) = a;
-    *reinterpret_cast<uint4 *>(s.x + tc::kmajor_offset(r, k + 8, IN)) = b;
+    const int r = tp >> 1, k = 16 * (tp & 1);
+    *reinterpret_cast<uint4 *>(x + tc::kmajor_offset(r, k, IN)) = a;
+    *reinterpret_cast<uint4 *>(x + tc::kmajor_offset(r, k + 8, IN)) = b;
 }
 
-// out[i] = (y0, y1, y2, 0) for n feature rows; persistent CTAs, tiles of 128
-// rows.  The next tile's features are fetched while the current one runs.
-__global__ void __launch_bounds__(kMlpThreads, kMlpCtasPerSm)
+// out[i] = (y0, y1, y2, 0) for n feature rows; tiles of 128 rows, pipeline
+// p of CTA b takes tiles (b kPipes + p) + k gridDim.x kPipes.  The next
+// tile's features are fetched while the current one runs.
+__global__ void __launch_bounds__(kMlpThreads, 1)
 k_mlp(int n, const __nv_bfloat16 *__restrict__ feat, const __nv_bfloat16 *__restrict__ wbf,
       const float *__restrict__ wf, float4 *__restrict__ out, unsigned *__restrict__ err)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    MlpSmem &s = *reinterpret_cast<MlpSmem *>(smem_raw);
-    const int t = threadIdx.x, w = t >> 5;
-    if (w == 0) {
-        tc::tmem_alloc(&s.taddr, kTmemCols);
+    MlpSmem &S = *reinterpret_cast<MlpSmem *>(smem_raw);
+    const int t = threadIdx.x;
+    const int p = t / kPipeThreads, tp = t % kPipeThreads, w = tp >> 5;
+    MlpPipe &P = S.pipe[p];
+    const int bar = 1 + p;
+    if (t < 32) {
+        tc::tmem_alloc(&S.w.taddr, kTmemCols);
         tc::tmem_relinquish();
     }
-    if (t == 0) {
-        tc::mbar_init(&s.mbar, 1);
+    if (tp == 0) {
+        tc::mbar_init(&P.mbar, 1);
         tc::mbar_fence_init();
     }
-    stage_weights(s, wbf, wf);
+    stage_weights(S.w, wbf, wf);
     const int ntiles = (n + 127) / 128;
+    const int stride = gridDim.x * kPipes;
+    int tile = blockIdx.x * kPipes + p;
     {
         uint4 a, b;
-        load_feat(feat, n, blockIdx.x, a, b);
-        store_feat(s, a, b);
+        load_feat(feat, n, tile, tp, a, b);
+        store_feat(P.x, tp, a, b);
     }
     tc::fence_async_smem();
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
-    const uint32_t tbase = s.taddr;
+    const uint32_t tacc = S.w.taddr + (uint32_t)(128 * p);
+    const uint32_t sx = tc::smem_u32(P.x), sh = tc::smem_u32(P.hbuf);
     uint32_t phase = 0;
     bool ok = true;
-    // `ok` stays uniform across the CTA (every barrier after a wait is a
-    // vote), so a wait that gives up ends the loop in all threads together.
-    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        // layer 1: x (128 x 32) . W1^T -> TMEM [0, 128)
-        if (t == 0) {
-            tc::mma_tile(tbase, tc::smem_u32(s.x), tc::smem_u32(s.w1), HID, IN, false);
-            tc::mma_commit(&s.mbar);
+    // `ok` stays uniform across the pipeline (every barrier after a wait is
+    // a vote), so a wait that gives up ends its loop in all its threads.
+    for (; tile < ntiles; tile += stride) {
+        // layer 1: x (128 x 32) . W1'^T
+        if (tp == 0) {
+            tc::mma_tile(tacc, sx, tc::smem_u32(S.w.w1), HID, IN, false);
+            tc::mma_commit(&P.mbar);
         }
         uint4 na, nb;
-        load_feat(feat, n, tile + gridDim.x, na, nb);
-        bool done = tc::mbar_wait(&s.mbar, phase);
+        load_feat(feat, n, tile + stride, tp, na, nb);
+        bool done = tc::mbar_wait(&P.mbar, phase);
         phase ^= 1u;
         tc::fence_after_sync();
-        store_feat(s, na, nb);  // layer 1 has consumed x
-        hidden_epilogue(s, tbase, 0, s.b1);
+        store_feat(P.x, tp, na, nb);  // layer 1 has consumed x
+        hidden_epilogue(P.hbuf, tacc, tp);
         tc::fence_async_smem();
         tc::fence_before_sync();
-        ok = __syncthreads_and(done) != 0;
+        ok = tc::named_sync_and(bar, kPipeThreads, done);
         tc::fence_after_sync();
         if (!ok) break;
-        // layer 2: h1 (128 x 128) . W2^T -> TMEM [128, 256)
-        if (t == 0) {
-            tc::mma_tile(tbase + HID, tc::smem_u32(s.hbuf), tc::smem_u32(s.w2), HID, HID, false);
-            tc::mma_commit(&s.mbar);
+        // layer 2: h1 (128 x 128) . W2^T + 1 . b2^T
+        if (tp == 0) {
+            tc::mma_tile(tacc, sh, tc::smem_u32(S.w.w2), HID, HID, false);
+            tc::mma_tile(tacc, tc::smem_u32(S.w.ones), tc::smem_u32(S.w.w2b), HID, 16, true);
+            tc::mma_commit(&P.mbar);
         }
-        done = tc::mbar_wait(&s.mbar, phase);
+        done = tc::mbar_wait(&P.mbar, phase);
         phase ^= 1u;
         tc::fence_before_sync();
-        ok = __syncthreads_and(done) != 0;  // hbuf is consumed before it is overwritten
+        ok = tc::named_sync_and(bar, kPipeThreads, done);  // hbuf consumed before it is rewritten
         tc::fence_after_sync();
         if (!ok) break;
-        hidden_epilogue(s, tbase, HID, s.b2);
+        hidden_epilogue(P.hbuf, tacc, tp);
         tc::fence_async_smem();
         tc::fence_before_sync();
-        __syncthreads();
+        tc::named_sync(bar, kPipeThreads);
         tc::fence_after_sync();
-        // layer 3: h2 (128 x 128) . W3^T -> TMEM [0, 16)
-        if (t == 0) {
-            tc::mma_tile(tbase, tc::smem_u32(s.hbuf), tc::smem_u32(s.w3), OUT, HID, false);
-            tc::mma_commit(&s.mbar);
+        // layer 3: h2 (128 x 128) . W3^T -> columns [0, 16)
+        if (tp == 0) {
+            tc::mma_tile(tacc, sh, tc::smem_u32(S.w.w3), OUT, HID, false);
+            tc::mma_commit(&P.mbar);
         }
-        done = tc::mbar_wait(&s.mbar, phase);
+        done = tc::mbar_wait(&P.mbar, phase);
         phase ^= 1u;
         tc::fence_after_sync();
         if (w < 4) {
             float v[16];
-            tc::tmem_ld16(tbase + ((uint32_t)(32 * w) << 16), v);
-            const int gi = tile * 128 + 32 * w + (t & 31);
+            tc::tmem_ld16(tacc + ((uint32_t)(32 * w) << 16), v);
+            const int gi = tile * 128 + 32 * w + (tp & 31);
             if (gi < n && done)
-                __stcs(out + gi, make_float4(v[0] + s.b3[0], v[1] + s.b3[1], v[2] + s.b3[2], 0.0f));
+                __stcs(out + gi, make_float4(v[0] + S.w.b3[0], v[1] + S.w.b3[1], v[2] + S.w.b3[2], 0.0f));
         }
         tc::fence_before_sync();
-        ok = __syncthreads_and(done) != 0;  // TMEM [0, 16) read before layer 1 reuses it
+        ok = tc::named_sync_and(bar, kPipeThreads, done);  // read before layer 1 reuses it
         tc::fence_after_sync();
         if (!ok) break;
     }
-    if (!ok && t == 0) atomicAdd(err, 1u);
+    if (!ok && tp == 0) atomicAdd(err, 1u);
     tc::fence_before_sync();
     __syncthreads();
-    if (w == 0) tc::tmem_dealloc(tbase, kTmemCols);
+    if (t < 32) tc::tmem_dealloc(S.w.taddr, kTmemCols);
 }
 
 // ---------------------------------------------------------------------------
@@ -500,19 +541,21 @@ k_gemm(int M, int N, int K, const __nv_bfloat16 *__restrict__ A, long long sam, 
 // elementwise training kernels
 // ---------------------------------------------------------------------------
 
-// Z (rows x cols, FP32 pre-activation without bias) -> Zb = Z + b (kept),
-// H = GELU(Zb) in BF16, computed as the inference kernel computes it.
-// One thread per pair of columns (cols even).
-__global__ void k_bias_gelu(int rows, int cols, float *__restrict__ Z, const float *__restrict__ b,
-                            __nv_bfloat16 *__restrict__ H)
+// Z (rows x cols, FP32 pre-activation without bias) -> Zb = Z + bf16(b)
+// (kept), H = act(Zb) = 2 GELU(Zb) in BF16, computed as the inference kernel
+// computes it (which adds the bias in BF16 through the tensor cores).  One
+// thread per pair of columns (cols even).
+__global__ void k_bias_act(int rows, int cols, float *__restrict__ Z, const float *__restrict__ b,
+                           __nv_bfloat16 *__restrict__ H)
 {
     const long long e = 2 * ((long long)blockIdx.x * blockDim.x + threadIdx.x);
     if (e >= (long long)rows * cols) return;
     const int c = (int)(e % cols);
-    const float z0 = Z[e] + b[c], z1 = Z[e + 1] + b[c + 1];
+    const float z0 = Z[e] + __bfloat162float(__float2bfloat16(b[c]));
+    const float z1 = Z[e + 1] + __bfloat162float(__float2bfloat16(b[c + 1]));
     Z[e] = z0;
     Z[e + 1] = z1;
-    *reinterpret_cast<uint32_t *>(H + e) = tc::gelu_bf16x2(z0, z1);
+    *reinterpret_cast<uint32_t *>(H + e) = tc::act_bf16x2(z0, z1);
 }
 
 // Y += b3; dY = mask * 2 (Y - T) / rows (BF16); the squared error is added to *loss.
@@ -549,13 +592,13 @@ __global__ void k_out_grad(int rows, float *__restrict__ Y, const float *__restr
     }
 }
 
-// dZ = dH * GELU'(Zb) (BF16 out).
-__global__ void k_gelu_back(int rows, int cols, const float *__restrict__ dH,
+// dZ = dH * act'(Zb) (BF16 out).
+__global__ void k_act_back(int rows, int cols, const float *__restrict__ dH,
                             const float *__restrict__ Zb, __nv_bfloat16 *__restrict__ dZ)
 {
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= (long long)rows * cols) return;
-    dZ[e] = __float2bfloat16(dH[e] * gelu_grad(Zb[e]));
+    dZ[e] = __float2bfloat16(dH[e] * act_grad(Zb[e]));
 }
 
 // Column sums of a BF16 matrix (bias gradients), one thread per column.
@@ -835,9 +878,9 @@ int train_batch(LearnedModel *l, TrainBufs &b, int cmask, bool trunk, float lr)
     const __nv_bfloat16 *W1 = l->wbf + OFF_W1, *W2 = l->wbf + OFF_W2, *W3 = l->wbf + OFF_W3;
     // forward
     LTRY(gemm(st, B, HID, IN, b.Xb, IN, 1, W1, IN, 1, b.Z1, HID, l->d_err));
-    k_bias_gelu<<<nblk((long long)B * HID / 2), 256, 0, st>>>(B, HID, b.Z1, l->w + OFF_B1, b.H1);
+    k_bias_act<<<nblk((long long)B * HID / 2), 256, 0, st>>>(B, HID, b.Z1, l->w + OFF_B1, b.H1);
     LTRY(gemm(st, B, HID, HID, b.H1, HID, 1, W2, HID, 1, b.Z2, HID, l->d_err));
-    k_bias_gelu<<<nblk((long long)B * HID / 2), 256, 0, st>>>(B, HID, b.Z2, l->w + OFF_B2, b.H2);
+    k_bias_act<<<nblk((long long)B * HID / 2), 256, 0, st>>>(B, HID, b.Z2, l->w + OFF_B2, b.H2);
     LTRY(gemm(st, B, OUT, HID, b.H2, HID, 1, W3, HID, 1, b.Y, OUT, l->d_err));
     k_out_grad<<<nblk(B), 256, 0, st>>>(B, b.Y, l->w + OFF_B3, b.Tb, cmask, b.dY, b.loss);
     // backward: output layer
@@ -848,13 +891,13 @@ int train_batch(LearnedModel *l, TrainBufs &b, int cmask, bool trunk, float lr)
     if (trunk) {
         // dH2[b][h] = sum_o dY[b][o] W3[o][h]
         LTRY(gemm(st, B, HID, OUT, b.dY, OUT, 1, W3, 1, HID, b.dH2, HID, l->d_err));
-        k_gelu_back<<<nblk((long long)B * HID), 256, 0, st>>>(B, HID, b.dH2, b.Z2, b.dZ2);
+        k_act_back<<<nblk((long long)B * HID), 256, 0, st>>>(B, HID, b.dH2, b.Z2, b.dZ2);
         LTRY(gemm(st, HID, HID, B, b.dZ2, 1, HID, b.H1, 1, HID, l->g + OFF_W2, HID, l->d_err));
         k_colsum<<<1, HID, 0, st>>>(B, HID, b.dZ2, l->g + OFF_B2);
         LTRY(gemm(st, B, HID, HID, b.dZ2, HID, 1, W2, 1, HID, b.dH1, HID, l->d_err));
-        k_gelu_back<<<nblk((long long)B * HID), 256, 0, st>>>(B, HID, b.dH1, b.Z1, b.dZ1);
+        k_act_back<<<nblk((long long)B * HID), 256, 0, st>>>(B, HID, b.dH1, b.Z1, b.dZ1);
         LTRY(gemm(st, HID, IN, B, b.dZ1, 1, HID, b.Xb, 1, IN, l->g + OFF_W1, IN, l->d_err));
-        k_colsum<<<1, HID, 0, st>>>(B, HID, b.dZ1, l->g + OFF_B1);
+        // b1 stays zero: the first layer's bias is the weight of the constant feature 31
     }
     ++l->adam_t;
     const float b1t = powf(0.9f, (float)l->adam_t), b2t = powf(0.999f, (float)l->adam_t);
@@ -940,7 +983,7 @@ int run_mlp(cudaStream_t st, LearnedModel *l, int n, const __nv_bfloat16 *feat, 
     if (n == 0) return SPH_OK;
     LTRY(configure_kernels());
     const int ntiles = (n + 127) / 128;
-    const int grid = std::min(ntiles, ml::kMlpCtasPerSm * (sms > 0 ? sms : num_sms()));
+    const int grid = std::min((ntiles + ml::kPipes - 1) / ml::kPipes, sms > 0 ? sms : num_sms());
     ml::k_mlp<<<grid, ml::kMlpThreads, mlp_smem(), st>>>(n, feat, l->wbf, l->w, out, l->d_err);
     return cuda_fail(cudaGetLastError(), "mlp launch");
 }

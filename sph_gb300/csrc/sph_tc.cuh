@@ -170,24 +170,42 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32])
     for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// GELU (tanh form) of two values, computed in packed BF16 arithmetic:
-// x = bf16(a), bf16(b); y = x/2 (1 + tanh(x (c0 + c1 x^2))), c0 = sqrt(2/pi),
-// c1 = 0.044715 c0.  Returns the packed BF16 pair (a in the low half).
-__device__ __forceinline__ uint32_t gelu_bf16x2(float a, float b)
+// The network's activation of two values in packed BF16 arithmetic:
+// 2 GELU(x) = x (1 + tanh(x (c0 + c1 x^2))), c0 = sqrt(2/pi), c1 = 0.044715 c0,
+// x = bf16(a), bf16(b) (GELU in its tanh form, scaled by 2: the next layer's
+// weights absorb the factor).  Returns the packed pair (a in the low half).
+__device__ __forceinline__ uint32_t act_bf16x2(float a, float b)
 {
-    uint32_t x, x2, t, u, th, hx, y;
+    uint32_t x, x2, t, u, th, y;
     asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(x) : "f"(b), "f"(a));
-    const uint32_t c0 = 0x3F4C3F4Cu;  // bf16(0.7978846) x 2
-    const uint32_t c1 = 0x3D123D12u;  // bf16(0.0356774) x 2
-    const uint32_t half = 0x3F003F00u;
+    const uint32_t c0 = 0x3F4C3F4Cu;    // bf16(0.7978846) x 2
+    const uint32_t c1 = 0x3D123D12u;    // bf16(0.0356774) x 2
     const uint32_t zero = 0x80008000u;  // -0, the additive identity of fma
     asm("fma.rn.bf16x2 %0, %1, %2, %3;" : "=r"(x2) : "r"(x), "r"(x), "r"(zero));
     asm("fma.rn.bf16x2 %0, %1, %2, %3;" : "=r"(t) : "r"(x2), "r"(c1), "r"(c0));
     asm("fma.rn.bf16x2 %0, %1, %2, %3;" : "=r"(u) : "r"(x), "r"(t), "r"(zero));
     asm("tanh.approx.bf16x2 %0, %1;" : "=r"(th) : "r"(u));
-    asm("fma.rn.bf16x2 %0, %1, %2, %3;" : "=r"(hx) : "r"(x), "r"(half), "r"(zero));
-    asm("fma.rn.bf16x2 %0, %1, %2, %3;" : "=r"(y) : "r"(hx), "r"(th), "r"(hx));
+    asm("fma.rn.bf16x2 %0, %1, %2, %3;" : "=r"(y) : "r"(x), "r"(th), "r"(x));
     return y;
+}
+
+// Named barrier over `count` threads (ids 1..15; 0 is __syncthreads).
+__device__ __forceinline__ void named_sync(int id, int count)
+{
+    asm volatile("bar.sync %0, %1;" :: "r"(id), "r"(count) : "memory");
+}
+
+// Named barrier that also ANDs a predicate over the participating threads.
+__device__ __forceinline__ bool named_sync_and(int id, int count, bool v)
+{
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "bar.red.and.pred q, %2, %3, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(r) : "r"((uint32_t)v), "r"(id), "r"(count) : "memory");
+    return r != 0;
 }
 
 // D[128 x N] (+)= A[128 x K] . B[N x K]^T for operands staged in the

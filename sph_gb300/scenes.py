@@ -243,6 +243,112 @@ def learned_training_scenes(count: int = 200, n: int = 65_536, seed0: int = 4000
     return out
 
 
+def _reflect(v: np.ndarray, lo: float, hi: float) -> np.ndarray:
+    """Folds values back into [lo, hi] (two reflections, then a clip)."""
+    for _ in range(2):
+        v = np.where(v < lo, 2 * lo - v, v)
+        v = np.where(v > hi, 2 * hi - v, v)
+    return np.clip(v, lo, hi)
+
+
+def skewed_scene(seed: int, name: str, n_range=(512, 32768)) -> Scene:
+    """One scene of the skewed ensemble (config 5), before settling: N =
+    round(exp U(ln lo, ln hi)) particles in a box of area N h^2 (fill 0.25 at
+    the lattice spacing 0.5h) with aspect W/H ~ U[1, 2].  A fraction
+    U[0.5, 0.8] of them forms the pile: a jittered 0.5h lattice across the
+    whole box width from the floor.  The rest forms 1-6 Gaussian blobs
+    (sigma ~ U[3, 10]h, at most W/4, widened where needed so that the blob's
+    peak density stays at most 4 particles per h^2; with overlaps and
+    counting noise the fullest cells hold about 12), centred above the pile;
+    blob particles are kept in the box by reflection at the walls.  k ~
+    U[0.1, 0.5], k_near ~ U[1, 3], sigma ~ U[0, 1].  Scene randoms use
+    counters 0..15 of the seed (blob b: 8 + 2b, 9 + 2b; b < 4 share the rest
+    as rescaled draws), the lattice jitter the next 2 N_pile counters, the
+    blob offsets the 2 N_blob after them.  `x`, `y` hold the pile and
+    meta['blob_x'], meta['blob_y'] the blob particles."""
+    u = uniform(seed, np.arange(16, dtype=np.uint64))
+    lo, hi = math.log(n_range[0]), math.log(n_range[1])
+    n = int(round(math.exp(lo + (hi - lo) * u[0])))
+    nblobs = 1 + min(5, int(u[1] * 6))
+    pile_frac = 0.5 + 0.3 * u[2]
+    aspect = 1.0 + u[3]
+    p = Params(k=0.1 + 0.4 * u[4], k_near=1.0 + 2.0 * u[5], sigma=float(u[6]))
+    w = math.sqrt(n * aspect)
+    h_box = w / aspect
+    n_pile = int(round(n * pile_frac))
+    n_blob = n - n_pile
+    cols = max(1, int(w / 0.5) - 1)
+    i = np.arange(n_pile, dtype=np.int64)
+    row, col = np.divmod(i, cols)
+    ju = uniform(seed, np.arange(16, 16 + 2 * n_pile, dtype=np.uint64)).reshape(n_pile, 2)
+    x = (0.25 + col * 0.5 + (ju[:, 0] * 2.0 - 1.0) * 0.01).astype(np.float32)
+    y = (0.25 + row * 0.5 + (ju[:, 1] * 2.0 - 1.0) * 0.01).astype(np.float32)
+    pile_top = 0.25 + (int(row.max()) + 1 if n_pile else 0) * 0.5
+    # blobs
+    g = uniform(seed, np.arange(16 + 2 * n_pile, 16 + 2 * n_pile + 2 * n_blob,
+                                dtype=np.uint64)).reshape(max(n_blob, 0), 2)
+    r = np.sqrt(-2.0 * np.log(np.maximum(g[:, 0], 1e-300)))
+    gx, gy = r * np.cos(2 * math.pi * g[:, 1]), r * np.sin(2 * math.pi * g[:, 1])
+    counts = [n_blob // nblobs + (1 if b < n_blob % nblobs else 0) for b in range(nblobs)]
+    bx, by, o = [], [], 0
+    blobs = []
+    for b in range(nblobs):
+        ua, ub = (u[8 + 2 * b], u[9 + 2 * b]) if b < 4 else ((u[7] * (b + 1)) % 1.0, (u[15] * (b + 2)) % 1.0)
+        sig = min(3.0 + 7.0 * ua, w / 4.0)
+        sig = max(sig, math.sqrt(counts[b] / (2 * math.pi * 4.0)))
+        cx = sig + (w - 2 * sig) * ub if w > 2 * sig else w / 2
+        room = max(0.0, h_box - pile_top - 3 * sig)
+        cy = min(h_box - sig, pile_top + 1.5 * sig + room * ((ua + ub) % 1.0))
+        k = counts[b]
+        bx.append(_reflect(cx + sig * gx[o:o + k], 0.05, w - 0.05))
+        by.append(_reflect(cy + sig * gy[o:o + k], 0.05, h_box - 0.05))
+        blobs.append(dict(n=k, sigma=sig, centre=(cx, cy)))
+        o += k
+    p.node_start_x, p.node_end_x = 0.0, float(np.float32(w))
+    sc = Scene(name=name, x=x, y=y, vx=np.zeros(n_pile, np.float32), vy=np.zeros(n_pile, np.float32),
+               box=(0.0, float(np.float32(w)), 0.0, float(np.float32(h_box))), params=p, spacing=1.0,
+               size_x=int(math.ceil(float(np.float32(w)))), size_y=int(math.ceil(float(np.float32(h_box)))))
+    sc.meta = dict(n_total=n, n_pile=n_pile, pile_top=pile_top, blobs=blobs,
+                   blob_x=np.concatenate(bx).astype(np.float32) if bx else np.zeros(0, np.float32),
+                   blob_y=np.concatenate(by).astype(np.float32) if by else np.zeros(0, np.float32))
+    sc.steps = 500
+    return sc
+
+
+def config5(nscenes: int = 2048, n_range=(512, 32768)) -> list:
+    """The skewed ensemble before settling: 2,048 scenes (seeds 5000 + s)."""
+    return [skewed_scene(5000 + s, f"skewed_{s}", n_range) for s in range(nscenes)]
+
+
+SETTLE_STEPS = 300
+
+
+def settle_and_drop(piles: list, steps: int = SETTLE_STEPS) -> list:
+    """Settles every scene's pile with the plain method on the GPU (one
+    batched ensemble, `steps` steps, tunables of each scene), then adds the
+    blob particles at rest: the scenes of config 5."""
+    from .simulation import Ensemble
+    e = Ensemble(piles)
+    e.upload_scenes()
+    e.step(None, steps)
+    st = e.download()
+    e.close()
+    out = []
+    for k, sc in enumerate(piles):
+        sl = e.scene_slice(k)
+        bx, by = sc.meta["blob_x"], sc.meta["blob_y"]
+        nb = bx.shape[0]
+        full = Scene(name=sc.name, x=np.concatenate([st["x"][sl], bx]).astype(np.float32),
+                     y=np.concatenate([st["y"][sl], by]).astype(np.float32),
+                     vx=np.concatenate([st["v_x"][sl], np.zeros(nb, np.float32)]).astype(np.float32),
+                     vy=np.concatenate([st["v_y"][sl], np.zeros(nb, np.float32)]).astype(np.float32),
+                     box=sc.box, params=sc.params, spacing=sc.spacing, size_x=sc.size_x,
+                     size_y=sc.size_y, steps=sc.steps)
+        full.meta = dict(sc.meta, settle_steps=steps)
+        out.append(full)
+    return out
+
+
 def algorithmic_bytes_per_step(n: int, cells: int) -> int:
     """Canonical algorithmic HBM bytes of one step: 216 B per particle
     (viscosity+predict 40, cell build on predicted positions 68, density 16,

@@ -178,10 +178,12 @@ class Simulation:
         return counts[:self.n].copy(), ids[:total.value].copy()
 
     def _probe(self, fn, params):
-        t = tunables(params or self.params)
+        """params None: the handle's own tunables (each scene's, for an
+        ensemble)."""
+        t = None if params is None else ctypes.byref(tunables(params))
         a = np.zeros(self.n, np.float32)
         b = np.zeros(self.n, np.float32)
-        check(fn(self._h, ctypes.byref(t), _f(a), _f(b)))
+        check(fn(self._h, t, _f(a), _f(b)))
         return a, b
 
     def probe_density(self, params: dict | None = None):

@@ -18,9 +18,10 @@ def bf16(x):
     return ((u + r) & 0xFFFF0000).astype(np.uint32).view(np.float32)
 
 
-def gelu_bf16(z):
-    """GELU (tanh form) evaluated step by step in BF16 arithmetic, as the
-    kernels evaluate it (each fused multiply-add rounded once)."""
+def act_bf16(z):
+    """The network's activation, 2 GELU (tanh form), evaluated step by step
+    in BF16 arithmetic as the kernels evaluate it (each fused multiply-add
+    rounded once)."""
     r = lambda v: bf16(np.asarray(v, np.float32)).astype(np.float64)  # noqa: E731
     c0, c1 = r(0.7978846), r(0.0356774)
     x = r(z)
@@ -28,8 +29,7 @@ def gelu_bf16(z):
     t = r(x2 * c1 + c0)
     u = r(x * t)
     th = r(np.tanh(u))
-    hx = r(x * 0.5)
-    return r(hx * th + hx)
+    return r(x * th + x)
 
 
 @pytest.mark.parametrize("M,N,K", [(128, 128, 64), (200, 48, 96), (5, 16, 20), (300, 130, 130),
@@ -45,12 +45,16 @@ def test_gemm_matches_numpy(cuda_lib, M, N, K):
 
 
 def numpy_mlp(w, x):
+    """Inference form: the constant feature 31 carries the first bias, the
+    second bias is added in BF16."""
     p = LearnedModel.unpack(w)
+    W1 = p["W1"].astype(np.float32).copy()
+    W1[:, 31] = W1[:, 31] + p["b1"]
     xb = bf16(x).astype(np.float64)
-    z1 = xb @ bf16(p["W1"]).astype(np.float64).T + p["b1"]
-    h1 = gelu_bf16(z1)
-    z2 = h1 @ bf16(p["W2"]).astype(np.float64).T + p["b2"]
-    h2 = gelu_bf16(z2)
+    z1 = xb @ bf16(W1).astype(np.float64).T
+    h1 = act_bf16(z1)
+    z2 = h1 @ bf16(p["W2"]).astype(np.float64).T + bf16(p["b2"])
+    h2 = act_bf16(z2)
     return h2 @ bf16(p["W3"]).astype(np.float64).T + p["b3"]
 
 
@@ -62,6 +66,7 @@ def test_mlp_forward_matches_numpy(cuda_lib):
         m.set_params(w)
         assert np.array_equal(m.get_params(), w)
         x = rng.standard_normal((1000, LearnedModel.IN)).astype(np.float32)
+        x[:, 31] = 1.0  # the constant feature
         y = m.forward(x)
         ref = numpy_mlp(w, x)
         # tanh.approx against tanh: an occasional BF16 ulp in an activation
@@ -125,7 +130,7 @@ def numpy_features(sc):
              ak, an, as_, rest / 4,
              ak * (a - rest) * V1[0] / 4, ak * (a - rest) * V1[1] / 4,
              an * b * V2[0] / 2, an * b * V2[1] / 2, as_ * V1[0] / 2, as_ * V1[1] / 2]
-        f += [0.0] * (32 - len(f))
+        f += [0.0] * (31 - len(f)) + [1.0]
         out[i] = f
     return out, cnt
 

@@ -38,3 +38,37 @@ def test_ensemble_scene_statistics():
         assert s.size_x == math.ceil(s.box[1]) and s.size_y == math.ceil(s.box[3])
     again = scenes.config3(nscenes=3)
     assert all(np.array_equal(a.x, b.x) for a, b in zip(e[:3], again))
+
+
+def test_skewed_scene_statistics():
+    sc = scenes.config5(nscenes=48)
+    ns = np.array([s.meta["n_total"] for s in sc])
+    assert ns.min() >= 512 and ns.max() <= 32768
+    occ = []
+    for s in sc:
+        m = s.meta
+        assert s.n == m["n_pile"] and m["blob_x"].shape[0] == m["n_total"] - m["n_pile"]
+        assert 0.49 <= m["n_pile"] / m["n_total"] <= 0.81
+        assert 1 <= len(m["blobs"]) <= 6
+        for b in m["blobs"]:
+            assert b["sigma"] >= 3.0 or b["sigma"] >= s.box[1] / 4 - 1e-9
+        x = np.concatenate([s.x, m["blob_x"]])
+        y = np.concatenate([s.y, m["blob_y"]])
+        assert x.min() >= 0 and x.max() < s.box[1] and y.min() >= 0 and y.max() < s.box[3]
+        assert 1.0 <= s.box[1] / s.box[3] <= 2.0 + 1e-6
+        k = np.floor(y).astype(np.int64) * s.size_x + np.floor(x).astype(np.int64)
+        occ.append(np.bincount(k).max())
+    # cell occupancies up to about a dozen per h^2 cell, far below the 100 cap
+    assert 6 <= max(occ) <= 30
+    again = scenes.config5(nscenes=2)
+    assert all(np.array_equal(a.meta["blob_x"], b.meta["blob_x"]) for a, b in zip(sc[:2], again))
+
+
+def test_learned_training_scenes():
+    tr = scenes.learned_training_scenes(8, 65_536)
+    assert all(s.n == 65_536 for s in tr)
+    ks = [s.params.k for s in tr]
+    assert len(set(ks)) == 8 and all(0.1 <= k <= 0.5 for k in ks)
+    assert all(1.0 <= s.params.k_near <= 3.0 and 0.0 <= s.params.sigma <= 1.0 for s in tr)
+    assert all(s.mover_period == 0.0 for s in tr)
+    assert np.array_equal(tr[0].x, scenes.config2(65_536).x)
