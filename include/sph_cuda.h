@@ -98,6 +98,32 @@ typedef struct sph_scene_desc {
 int sph_cuda_create_ensemble(sph_cuda_t **out, const sph_scene_desc *scenes, int nscenes,
                              int max_bucket, int max_neighbors);
 
+/* ---- on-device scene initialisation ---- */
+
+/* A block of particles on a square lattice, generated on the GPU (replaces
+ * the host loops of constructFluidVolume / initParticles, geometry.c:29-67,
+ * fluid.c:747-768, for the synthetic scenes): particle k of the block sits
+ * at row k / cols, column k % cols,
+ *   x = float((x0 + column * spacing) + (2 u(2k) - 1) * jitter),
+ *   y = float((y0 + row * spacing) + (2 u(2k + 1) - 1) * jitter),
+ * with u(c) = top 53 bits of splitmix64(seed + (counter0 + c + 1) * golden)
+ * as a double in [0, 1), all in IEEE double arithmetic without fused
+ * multiply-adds, and velocity 0. */
+typedef struct sph_lattice_block {
+    int n;                       /* particles of the block */
+    int cols;                    /* particles per lattice row */
+    double x0, y0;               /* lower-left lattice point */
+    double spacing;              /* lattice spacing */
+    double jitter;               /* uniform jitter half-width per axis */
+    unsigned long long seed;     /* splitmix64 seed */
+    unsigned long long counter0; /* first counter of the block */
+} sph_lattice_block;
+
+/* Replaces the handle's particles by the concatenated blocks (ids in block
+ * order; for an ensemble, block s is scene s and the counts must match the
+ * scenes'), as an upload of the same values would. */
+int sph_cuda_init_lattice(sph_cuda_t *h, const sph_lattice_block *blocks, int nblocks);
+
 /* Sets scene `scene`'s tunables for the following steps (all handles). */
 int sph_cuda_set_scene_params(sph_cuda_t *h, int scene, const tunable_parameters *tp);
 
@@ -261,6 +287,44 @@ int sph_cuda_launches_per_step(sph_cuda_t *h);
  * records a second one, waits for it and returns the elapsed milliseconds. */
 int sph_cuda_timer_start(sph_cuda_t *h);
 int sph_cuda_timer_stop(sph_cuda_t *h, float *ms);
+
+/* ---- headless liquid-surface image ---- */
+
+/* The render rank's liquid drawing (draw_liquid, liquid_gl.c:305-447, and
+ * its shaders) as compute kernels, without a graphics API: metaball sprites
+ * of diameter 0.020 x width splatted additively into an 8-bit alpha texture
+ * at half the screen resolution, a 15-tap Gaussian blur along y then x,
+ * then the threshold/smoothstep composite over black at full resolution.
+ * rgb receives width x height x 3 bytes, top row first (a binary PPM body);
+ * alpha, if not NULL, the blurred (width/2) x (height/2) alpha texture,
+ * bottom row first.
+ *   sph_render_liquid        from packed short coordinates (the render
+ *                            rank's input, fluid.c:356-362), host memory
+ *   sph_cuda_render_liquid   from a handle's current particles (packed on
+ *                            the device, no host round trip) */
+int sph_render_liquid(const short *coords, int n, int width, int height, unsigned char *rgb,
+                      unsigned char *alpha);
+int sph_cuda_render_liquid(sph_cuda_t *h, int width, int height, unsigned char *rgb,
+                           unsigned char *alpha);
+
+/* ---- live tunables (host helpers, no device work) ---- */
+
+/* The render rank's fluid presets (controls.c:344-401), applied to a
+ * caller's tunables: 'x' standard fluid, 'y' "super goo", 'a' zero g with
+ * high surface tension, 'b' spring gas; each sets g, k, k_near, k_spring,
+ * sigma, beta and rest_density.  'm' resets the mover to 2 x 2
+ * (controls.c:333-339).  SPH_ERR_INVALID for any other letter.  The values
+ * reach the device with the next sph_cuda_step / sph_cuda_set_scene_params
+ * (a pinned-buffer copy between graph launches). */
+int sph_cuda_tunables_preset(tunable_parameters *tp, char which);
+
+/* One frame of the render rank's inactive-mode mover path
+ * (renderer.c:493-532): gl_x += 0.01 direction, direction reversed outside
+ * [-1, 1], gl_y = sin(3.14 * 5 gl_x) / 10 - 0.6, and the centre in
+ * simulation coordinates (renderer.c:397-404) for a box [0, max_x] x
+ * [0, max_y].  *gl_x and *direction carry the path's state between frames. */
+int sph_cuda_mover_track(float max_x, float max_y, float *gl_x, int *direction,
+                         float *center_x, float *center_y);
 
 /* Page-locked host memory for fast transfers (e.g. the packed coordinates
  * buffer of sph_cuda_pack_coords_short), and its release. */

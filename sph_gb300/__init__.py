@@ -6,6 +6,6 @@ wraps it for Python callers; it contains no CPU implementation of the step.
 """
 from . import scenes
 from ._lib import PARTICLE_DTYPE, SphError, lib
-from .simulation import Ensemble, LearnedModel, Simulation, gemm_check
+from .simulation import Ensemble, LearnedModel, Simulation, gemm_check, render_liquid, write_ppm
 
-__all__ = ["Simulation", "Ensemble", "LearnedModel", "gemm_check", "SphError", "PARTICLE_DTYPE", "scenes", "lib"]
+__all__ = ["Simulation", "Ensemble", "LearnedModel", "gemm_check", "render_liquid", "write_ppm", "SphError", "PARTICLE_DTYPE", "scenes", "lib"]

@@ -96,6 +96,13 @@ class SphError(RuntimeError):
         self.status = status
 
 
+class LatticeBlock(ctypes.Structure):
+    """sph_lattice_block (include/sph_cuda.h)."""
+    _fields_ = [("n", ctypes.c_int), ("cols", ctypes.c_int), ("x0", ctypes.c_double),
+                ("y0", ctypes.c_double), ("spacing", ctypes.c_double), ("jitter", ctypes.c_double),
+                ("seed", ctypes.c_ulonglong), ("counter0", ctypes.c_ulonglong)]
+
+
 _lib = None
 
 _P = ctypes.c_void_p
@@ -105,6 +112,14 @@ _SIGS = {
     "sph_cuda_destroy": (ctypes.c_int, [_P]),
     "sph_cuda_create_ensemble": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.POINTER(SceneDesc), ctypes.c_int,
                                                 ctypes.c_int, ctypes.c_int]),
+    "sph_render_liquid": (ctypes.c_int, [c_short_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                         ctypes.c_void_p, ctypes.c_void_p]),
+    "sph_cuda_render_liquid": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                              ctypes.c_void_p]),
+    "sph_cuda_tunables_preset": (ctypes.c_int, [ctypes.POINTER(TunableParameters), ctypes.c_char]),
+    "sph_cuda_mover_track": (ctypes.c_int, [ctypes.c_float, ctypes.c_float, c_float_p, c_int_p,
+                                            c_float_p, c_float_p]),
+    "sph_cuda_init_lattice": (ctypes.c_int, [_P, ctypes.POINTER(LatticeBlock), ctypes.c_int]),
     "sph_cuda_set_scene_params": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(TunableParameters)]),
     "sph_cuda_num_scenes": (ctypes.c_int, [_P]),
     "sph_cuda_scene_diagnostics": (ctypes.c_int, [_P, c_double_p]),

@@ -20,6 +20,8 @@ INCLUDE = os.path.join(ROOT, "include")
 OBJ = os.path.join(ROOT, "_build")
 LIB_DIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIB_DIR, "libsph_cuda.so")
+HOST = os.path.join(PKG, "host")
+COMPUTE_RANK = os.path.join(LIB_DIR, "sph_compute_rank")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2",
@@ -42,8 +44,23 @@ def _stale() -> bool:
         return True
     t = os.path.getmtime(LIB)
     deps = sources() + glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(CSRC, "*.cuh")) \
-        + glob.glob(os.path.join(INCLUDE, "*.h")) + [os.path.abspath(__file__)]
-    return any(os.path.getmtime(d) > t for d in deps)
+        + glob.glob(os.path.join(INCLUDE, "*.h")) + glob.glob(os.path.join(HOST, "*.c")) \
+        + [os.path.abspath(__file__)]
+    return not os.path.exists(COMPUTE_RANK) or any(os.path.getmtime(d) > t for d in deps)
+
+
+def build_host(verbose: bool = False) -> str:
+    """The C compute-rank program (sph_gb300/host/compute_rank.c) linked
+    against libsph_cuda, next to it."""
+    cc = os.environ.get("CC", "gcc")
+    cmd = [cc, "-std=c99", "-O2", "-Wall", "-I", INCLUDE, os.path.join(HOST, "compute_rank.c"),
+           "-L", LIB_DIR, "-lsph_cuda", "-Wl,-rpath,$ORIGIN", "-lm", "-o", COMPUTE_RANK]
+    if verbose:
+        print(" ".join(cmd), file=sys.stderr)
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+    if r.returncode != 0:
+        raise RuntimeError("host program build failed:\n" + r.stdout.decode(errors="replace"))
+    return COMPUTE_RANK
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
@@ -79,6 +96,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError("nvcc link failed:\n" + r.stdout.decode(errors="replace"))
     os.replace(tmp, LIB)
+    build_host(verbose)
     return LIB
 
 

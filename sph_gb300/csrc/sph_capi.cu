@@ -3,6 +3,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
+#include <cmath>
 #include <cstring>
 #include <new>
 
@@ -977,6 +978,60 @@ int sph_cuda_host_alloc(void **ptr, size_t bytes)
 int sph_cuda_host_free(void *ptr)
 {
     if (ptr) SPH_CUDA(cudaFreeHost(ptr));
+    return SPH_OK;
+}
+
+int sph_cuda_tunables_preset(tunable_parameters *tp, char which)
+{
+    if (!tp) {
+        set_error("null tunables");
+        return SPH_ERR_INVALID;
+    }
+    struct Preset {
+        char id;
+        float g, k, k_near, k_spring, sigma, beta, rest;
+    };
+    // the render rank's presets, controls.c:344-401
+    static const Preset presets[] = {
+        {'x', 6.0f, 0.2f, 6.0f, 10.0f, 5.0f, 0.5f, 30.0f},
+        {'y', 6.0f, 0.1f, 3.0f, -30.0f, 100.0f, 10.0f, 30.0f},
+        {'a', 0.0f, 0.2f, 6.0f, 10.0f, 20.0f, 2.0f, 55.0f},
+        {'b', 6.0f, 0.0f, 0.0f, 115.0f, 20.0f, 2.0f, 0.0f},
+    };
+    if (which == 'm') {
+        tp->mover_width = 2.0f;
+        tp->mover_height = 2.0f;
+        return SPH_OK;
+    }
+    for (const Preset &p : presets)
+        if (p.id == which) {
+            tp->g = p.g;
+            tp->k = p.k;
+            tp->k_near = p.k_near;
+            tp->k_spring = p.k_spring;
+            tp->sigma = p.sigma;
+            tp->beta = p.beta;
+            tp->rest_density = p.rest;
+            return SPH_OK;
+        }
+    set_error("unknown preset '%c' (x, y, a, b or m)", which);
+    return SPH_ERR_INVALID;
+}
+
+int sph_cuda_mover_track(float max_x, float max_y, float *gl_x, int *direction, float *center_x,
+                         float *center_y)
+{
+    if (!gl_x || !direction || !center_x || !center_y) {
+        set_error("null argument");
+        return SPH_ERR_INVALID;
+    }
+    float x = *gl_x + 0.01f * (float)*direction;
+    if (x > 1.0f || x < -1.0f) *direction = -*direction;
+    const float y = sinf(3.14f * 5.0f * x) / 10.0f - 0.6f;
+    *gl_x = x;
+    const float hw = max_x * 0.5f, hh = max_y * 0.5f;
+    *center_x = x * hw + hw;
+    *center_y = y * hh + hh;
     return SPH_OK;
 }
 

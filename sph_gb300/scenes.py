@@ -143,6 +143,8 @@ def dam_break(n: int, cols: int, box_w: float, box_h: float, seed: int, *, name:
     sc = Scene(name=name, x=x, y=y, vx=np.zeros(n, np.float32), vy=np.zeros(n, np.float32),
                box=(0.0, float(box_w), 0.0, float(box_h)), params=p, spacing=h,
                size_x=int(math.ceil(box_w / h)), size_y=int(math.ceil(box_h / h)))
+    sc.meta = dict(lattice=dict(n=n, cols=cols, x0=float(x0), y0=float(y0), spacing=float(lattice),
+                                jitter=float(jitter), seed=int(seed), counter0=0))
     return sc
 
 
@@ -211,7 +213,9 @@ def ensemble_scene(seed: int, name: str, n_range=(1024, 65536)) -> Scene:
     sc = Scene(name=name, x=x, y=y, vx=np.zeros(n, np.float32), vy=np.zeros(n, np.float32),
                box=(0.0, float(bw), 0.0, float(bh)), params=p, spacing=1.0,
                size_x=int(math.ceil(float(bw))), size_y=int(math.ceil(float(bh))))
-    sc.meta = dict(aspect=a, fill=f)
+    sc.meta = dict(aspect=a, fill=f,
+                   lattice=dict(n=n, cols=cols, x0=float(x0), y0=float(y0), spacing=0.5, jitter=0.01,
+                                seed=int(seed), counter0=8))
     return sc
 
 
@@ -309,6 +313,8 @@ def skewed_scene(seed: int, name: str, n_range=(512, 32768)) -> Scene:
                box=(0.0, float(np.float32(w)), 0.0, float(np.float32(h_box))), params=p, spacing=1.0,
                size_x=int(math.ceil(float(np.float32(w)))), size_y=int(math.ceil(float(np.float32(h_box)))))
     sc.meta = dict(n_total=n, n_pile=n_pile, pile_top=pile_top, blobs=blobs,
+                   lattice=dict(n=n_pile, cols=cols, x0=0.25, y0=0.25, spacing=0.5, jitter=0.01,
+                                seed=int(seed), counter0=16),
                    blob_x=np.concatenate(bx).astype(np.float32) if bx else np.zeros(0, np.float32),
                    blob_y=np.concatenate(by).astype(np.float32) if by else np.zeros(0, np.float32))
     sc.steps = 500
@@ -344,7 +350,8 @@ def settle_and_drop(piles: list, steps: int = SETTLE_STEPS) -> list:
                      vy=np.concatenate([st["v_y"][sl], np.zeros(nb, np.float32)]).astype(np.float32),
                      box=sc.box, params=sc.params, spacing=sc.spacing, size_x=sc.size_x,
                      size_y=sc.size_y, steps=sc.steps)
-        full.meta = dict(sc.meta, settle_steps=steps)
+        full.meta = {k: v for k, v in sc.meta.items() if k != "lattice"}
+        full.meta["settle_steps"] = steps
         out.append(full)
     return out
 

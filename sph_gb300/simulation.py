@@ -86,6 +86,17 @@ class Simulation:
         check(lib().sph_cuda_upload_soa(self._h, *[None if a is None else _f(a) for a in arrs], n))
         self.n = n
 
+    def init_lattice(self, blocks: list):
+        """Generates the particles on the GPU (sph_cuda_init_lattice) from
+        lattice-block dicts (n, cols, x0, y0, spacing, jitter, seed,
+        counter0), e.g. the `lattice` entry of a synthetic scene's meta."""
+        arr = (_lib.LatticeBlock * len(blocks))()
+        for a, b in zip(arr, blocks):
+            for k, _ in _lib.LatticeBlock._fields_:
+                setattr(a, k, b[k])
+        check(lib().sph_cuda_init_lattice(self._h, arr, len(blocks)))
+        self.n = sum(int(b["n"]) for b in blocks)
+
     def upload_particles(self, particles: np.ndarray):
         """particles: structured array of PARTICLE_DTYPE (fluid_particle)."""
         a = np.ascontiguousarray(particles, PARTICLE_DTYPE)
@@ -218,6 +229,16 @@ class Simulation:
         return float(ms.value)
 
 
+    def render_liquid(self, width: int = 1920, height: int = 1080, alpha: bool = False):
+        """The render rank's liquid image of the current particles:
+        (height, width, 3) uint8, top row first; with alpha=True also the
+        blurred half-resolution alpha texture (bottom row first)."""
+        rgb = np.zeros((height, width, 3), np.uint8)
+        a = np.zeros((height // 2, width // 2), np.uint8) if alpha else None
+        check(lib().sph_cuda_render_liquid(self._h, int(width), int(height), rgb.ctypes.data,
+                                           a.ctypes.data if alpha else None))
+        return (rgb, a) if alpha else rgb
+
     # -- learned relaxation -------------------------------------------------
     def set_learned(self, model: "LearnedModel | None", threshold: float = 0.01):
         """Attaches a trained model (None detaches): particles whose
@@ -329,6 +350,25 @@ class LearnedModel:
             out[name] = w[o:o + k].reshape(shp)
             o += k
         return out
+
+
+def render_liquid(coords: np.ndarray, width: int = 1920, height: int = 1080):
+    """The liquid image (and the half-resolution alpha texture) from packed
+    short coordinates [n, 2] (sph_render_liquid)."""
+    c = np.ascontiguousarray(coords, np.int16)
+    rgb = np.zeros((height, width, 3), np.uint8)
+    a = np.zeros((height // 2, width // 2), np.uint8)
+    check(lib().sph_render_liquid(c.ctypes.data_as(_lib.c_short_p), int(c.shape[0]), int(width),
+                                  int(height), rgb.ctypes.data, a.ctypes.data))
+    return rgb, a
+
+
+def write_ppm(path: str, rgb: np.ndarray):
+    """Binary PPM (P6) of an RGB8 image, top row first."""
+    h, w, _ = rgb.shape
+    with open(path, "wb") as f:
+        f.write(b"P6\n%d %d\n255\n" % (w, h))
+        f.write(np.ascontiguousarray(rgb, np.uint8).tobytes())
 
 
 def gemm_check(A: np.ndarray, B: np.ndarray) -> np.ndarray:

@@ -190,22 +190,81 @@ def rms_density_error(sc, model, state_steps, threshold):
         return float(np.sqrt(np.mean((ra - rb) ** 2)) / sc.params.rest_density), used / sc.n
 
 
-def test_training_and_learned_step(cuda_lib):
+@pytest.fixture(scope="module")
+def trained(cuda_lib):
+    """A model trained on one 16,384-particle dam break (samples every 8
+    steps over 240 steps), with the first and last training losses."""
     sc = dam_break()
-    with LearnedModel(400_000, seed=7) as m:
-        with Simulation.from_scene(sc) as s:
-            for t in range(0, 240, 8):
-                s.step_schedule([sc.params_at(t + i).as_dict() for i in range(8)])
-                m.collect(s, 0.6)
-        assert m.num_samples > 100_000
-        first = m.train(1, 2048, 1e-3)
-        last = m.train(12, 2048, 1e-3)
-        assert last < 0.5 * first, (first, last)
-        with Simulation.from_scene(sc) as s:
-            s.step_schedule([sc.params_at(i).as_dict() for i in range(200)])
-            m.calibrate(s, epochs=4)
-        err, frac = rms_density_error(sc, m, 200, 0.01)
-        err_all, frac_all = rms_density_error(sc, m, 200, 1e9)
-        assert frac_all > 0.7
-        assert err <= err_all + 1e-6
-        assert err <= 0.01, (err, frac, err_all)
+    m = LearnedModel(400_000, seed=7)
+    with Simulation.from_scene(sc) as s:
+        for t in range(0, 240, 8):
+            s.step_schedule([sc.params_at(t + i).as_dict() for i in range(8)])
+            m.collect(s, 0.6)
+    n = m.num_samples
+    first = m.train(1, 2048, 1e-3)
+    last = m.train(12, 2048, 1e-3)
+    with Simulation.from_scene(sc) as s:
+        s.step_schedule([sc.params_at(i).as_dict() for i in range(200)])
+        m.calibrate(s, epochs=4)
+    yield m, n, first, last
+    m.close()
+
+
+def test_training_and_learned_step(trained):
+    m, n, first, last = trained
+    sc = dam_break()
+    assert n > 100_000
+    assert last < 0.5 * first, (first, last)
+    err, frac = rms_density_error(sc, m, 200, 0.01)
+    err_all, frac_all = rms_density_error(sc, m, 200, 1e9)
+    assert frac_all > 0.7
+    assert err <= err_all + 1e-6
+    assert err <= 0.01, (err, frac, err_all)
+
+
+def test_params_round_trip_gives_the_same_steps(trained):
+    m = trained[0]
+    sc = dam_break()
+    w = m.get_params()
+    with LearnedModel(0, seed=99) as m2:
+        m2.set_params(w)
+        outs = []
+        for model in (m, m2):
+            with Simulation.from_scene(sc) as s:
+                s.step_schedule([sc.params_at(i).as_dict() for i in range(20)])
+                s.set_learned(model, 0.01)
+                s.step_schedule([sc.params_at(20 + i).as_dict() for i in range(5)])
+                outs.append(s.download())
+        for f in ("x", "y", "v_x", "v_y"):
+            assert bits_equal(outs[0][f], outs[1][f]), f
+
+
+def test_skewed_ensemble_learned(trained):
+    """Config-5 scenes (settled piles + Gaussian blobs), batched, with the
+    network: one step against the plain ensemble from the same state."""
+    from sph_gb300 import Ensemble
+    m = trained[0]
+    scs = scenes.settle_and_drop(scenes.config5(12), 60)
+    n = sum(s.n for s in scs)
+    a, b = Ensemble(scs), Ensemble(scs)
+    try:
+        for e in (a, b):
+            e.upload_scenes()
+            e.step(None, 30)
+        b.set_learned(m, 0.01)
+        a.step(None, 1)
+        b.step(None, 1)
+        ra, _ = a.probe_density()
+        rb, _ = b.probe_density()
+        used, fell = b.learned_counts()
+        assert used + fell == n and used > 0.5 * n
+        rms = float(np.sqrt(np.mean((ra.astype(np.float64) - rb) ** 2)) / 1.3)
+        assert rms <= 0.01, rms
+        # every scene stays in its box
+        st = b.download()
+        for k, sc in enumerate(scs):
+            sl = b.scene_slice(k)
+            assert st["x"][sl].min() >= 0 and st["x"][sl].max() <= sc.box[1]
+    finally:
+        a.close()
+        b.close()
