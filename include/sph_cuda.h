@@ -198,6 +198,16 @@ int sph_cuda_download_soa(sph_cuda_t *h, float *x, float *y, float *vx, float *v
  * stays with the caller). */
 int sph_cuda_pack_coords_short(sph_cuda_t *h, short *coords, int n);
 
+/* The same packing without waiting: the packed coordinates of the current
+ * state are copied into `coords` (page-locked, e.g. from
+ * sph_cuda_host_alloc) on a separate copy stream, so the copy overlaps the
+ * next sph_cuda_step; sph_cuda_coords_wait(h, coords) returns once they
+ * have arrived.  Two copies may be in flight (alternate two buffers, as the
+ * reference overlaps its MPI_Isend with the next steps, fluid.c:282-287,
+ * 356-364); a third call waits for the oldest. */
+int sph_cuda_pack_coords_async(sph_cuda_t *h, short *coords, int n);
+int sph_cuda_coords_wait(sph_cuda_t *h, const short *coords);
+
 /* Rebuilds the neighbour relation on the current positions, like
  * hash_fluid(.., false) (fluid.c:341): after it, the next step applies
  * viscosity impulses even if it is the first step after an upload. */

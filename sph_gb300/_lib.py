@@ -136,6 +136,8 @@ _SIGS = {
     "sph_cuda_download_particles": (ctypes.c_int, [_P, _P, ctypes.c_int]),
     "sph_cuda_download_soa": (ctypes.c_int, [_P] + [c_float_p] * 6 + [ctypes.c_int]),
     "sph_cuda_pack_coords_short": (ctypes.c_int, [_P, c_short_p, ctypes.c_int]),
+    "sph_cuda_pack_coords_async": (ctypes.c_int, [_P, c_short_p, ctypes.c_int]),
+    "sph_cuda_coords_wait": (ctypes.c_int, [_P, c_short_p]),
     "sph_cuda_rebuild_neighbors": (ctypes.c_int, [_P]),
     "sph_cuda_synchronize": (ctypes.c_int, [_P]),
     "sph_cuda_get_counters": (ctypes.c_int, [_P, ctypes.POINTER(Counters)]),

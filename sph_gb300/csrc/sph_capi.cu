@@ -183,6 +183,13 @@ static void free_all(sph_cuda *h)
 {
     destroy_graph(h);
     free_learned_buffers(h);
+    if (h->copy_stream) cudaStreamSynchronize(h->copy_stream);
+    for (int k = 0; k < 2; ++k) {
+        if (h->d_coords[k]) cudaFree(h->d_coords[k]);
+        if (h->pack_ev[k]) cudaEventDestroy(h->pack_ev[k]);
+        if (h->copy_ev[k]) cudaEventDestroy(h->copy_ev[k]);
+    }
+    if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
     void *ptrs[] = {h->pos_a, h->vel_a, h->id_a, h->pos_b, h->prev_b, h->vel_b, h->kr_b,
                     h->pos_c, h->prev_c, h->xr_c, h->mask01_c, h->mask2_c, h->id_c,
                     h->tmp_id, h->cnt, h->start_a, h->start_c, h->tile_sums, h->d_scenes,
@@ -656,6 +663,49 @@ int sph_cuda_pack_coords_short(sph_cuda_t *h, short *coords, int n)
     if (n > 0) SPH_CUDA(cudaMemcpyAsync(coords, h->d_scratch, b, cudaMemcpyDeviceToHost, h->stream));
     SPH_CUDA(cudaStreamSynchronize(h->stream));
     return SPH_OK;
+}
+
+int sph_cuda_pack_coords_async(sph_cuda_t *h, short *coords, int n)
+{
+    SPH_TRY(check_handle(h));
+    if (n != h->n || (!coords && n > 0)) {
+        set_error("pack: n %d (handle holds %d) or null buffer", n, h->n);
+        return SPH_ERR_INVALID;
+    }
+    if (!h->copy_stream) {
+        SPH_CUDA(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+        for (int k = 0; k < 2; ++k) {
+            SPH_CUDA(cudaMalloc(&h->d_coords[k], ((size_t)h->capacity + 1) * sizeof(short2)));
+            SPH_CUDA(cudaEventCreateWithFlags(&h->pack_ev[k], cudaEventDisableTiming));
+            SPH_CUDA(cudaEventCreateWithFlags(&h->copy_ev[k], cudaEventDisableTiming));
+        }
+    }
+    const int k = h->pack_slot;
+    // the copy made from this staging buffer two calls ago must be complete
+    if (h->copy_dst[k]) SPH_CUDA(cudaEventSynchronize(h->copy_ev[k]));
+    SPH_TRY(launch_pack(h, h->d_coords[k]));
+    SPH_CUDA(cudaEventRecord(h->pack_ev[k], h->stream));
+    SPH_CUDA(cudaStreamWaitEvent(h->copy_stream, h->pack_ev[k], 0));
+    if (n > 0)
+        SPH_CUDA(cudaMemcpyAsync(coords, h->d_coords[k], (size_t)n * sizeof(short2),
+                                 cudaMemcpyDeviceToHost, h->copy_stream));
+    SPH_CUDA(cudaEventRecord(h->copy_ev[k], h->copy_stream));
+    h->copy_dst[k] = coords;
+    h->pack_slot = k ^ 1;
+    return SPH_OK;
+}
+
+int sph_cuda_coords_wait(sph_cuda_t *h, const short *coords)
+{
+    SPH_TRY(check_handle(h));
+    for (int k = 0; k < 2; ++k)
+        if (h->copy_dst[k] && h->copy_dst[k] == (const void *)coords) {
+            SPH_CUDA(cudaEventSynchronize(h->copy_ev[k]));
+            h->copy_dst[k] = nullptr;
+            return SPH_OK;
+        }
+    set_error("no pending coordinate copy into %p", (const void *)coords);
+    return SPH_ERR_STATE;
 }
 
 int sph_cuda_rebuild_neighbors(sph_cuda_t *h)

@@ -148,6 +148,15 @@ struct sph_cuda {
     int graph_n = -1;
     cudaEvent_t timer[2] = {nullptr, nullptr};
     int launches_per_step = 0;
+
+    // asynchronous coordinate hand-off: two device staging buffers, copied to
+    // the caller's host buffers on their own stream
+    cudaStream_t copy_stream = nullptr;
+    short2 *d_coords[2] = {nullptr, nullptr};
+    cudaEvent_t pack_ev[2] = {nullptr, nullptr};
+    cudaEvent_t copy_ev[2] = {nullptr, nullptr};
+    const void *copy_dst[2] = {nullptr, nullptr};
+    int pack_slot = 0;
 };
 
 namespace sph {

@@ -124,6 +124,14 @@ class Simulation:
         return out
 
     # -- stepping ------------------------------------------------------------
+    def pack_coords_async(self, out: np.ndarray):
+        """Starts the packed-coordinate copy into `out` ([n, 2] int16,
+        page-locked); wait_coords(out) completes it."""
+        check(lib().sph_cuda_pack_coords_async(self._h, out.ctypes.data_as(_lib.c_short_p), self.n))
+
+    def wait_coords(self, out: np.ndarray):
+        check(lib().sph_cuda_coords_wait(self._h, out.ctypes.data_as(_lib.c_short_p)))
+
     def step(self, params: dict | None = None, nsteps: int = 1):
         t = tunables(params or self.params)
         check(lib().sph_cuda_step(self._h, ctypes.byref(t), int(nsteps)))
