@@ -4,10 +4,11 @@
  * (fluid.c:541-611), which stays as the fallback and the judge.
  *
  * Model.  A message-passing network over each particle's neighbours within h
- * (at most 48 of them): messages are the neighbour offsets, relative
- * velocities, densities and near densities, weighted by (1 - r/h)^p and
- * aggregated into a 32-wide feature row (together with the particle's own
- * densities and its scene's stiffness ratios); a 2-layer width-128 GELU MLP
+ * (particles with more than 48 take the plain relaxation): messages are the
+ * neighbour offsets and relative velocities, weighted by (1 - r/h)^p and
+ * aggregated into a 32-wide feature row, joined with the particle's own
+ * density and near density and its scene's stiffness ratios; a 2-layer
+ * width-128 GELU MLP
  * maps the row to the relaxation displacement (in units of
  * s = h dt^2 (k + k_near + k_spring)) and to a predicted density error.
  * BF16 weights and activations, FP32 accumulation, on the tcgen05 tensor
@@ -83,6 +84,13 @@ int sph_learned_features(sph_cuda_t *h, float *features, int *counts);
 /* C[M x N] = A[M x K] . B[N x K]^T on the tcgen05 tensor cores, from FP32
  * host matrices rounded to BF16 (row-major), FP32 result.  For tests. */
 int sph_learned_gemm_check(const float *A, const float *B, float *C, int M, int N, int K);
+
+/* Every wait of the tensor-core kernels on an mbarrier is bounded (one
+ * second of the GPU's global timer): a wait that gives up ends its kernel
+ * with an error status
+ * instead of hanging the GPU.  This runs one such wait on an mbarrier that
+ * nothing arrives at; *gave_up = 1 when the bound worked. */
+int sph_learned_wait_selftest(int *gave_up);
 
 /* Attaches (or, with l == NULL, detaches) a trained model to a handle;
  * threshold is the largest predicted density error, in units of the rest

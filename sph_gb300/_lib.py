@@ -171,6 +171,7 @@ _SIGS = {
     "sph_learned_set_params": (ctypes.c_int, [_P, c_float_p]),
     "sph_learned_forward": (ctypes.c_int, [_P, c_float_p, ctypes.c_int, c_float_p]),
     "sph_learned_features": (ctypes.c_int, [_P, c_float_p, c_int_p]),
+    "sph_learned_wait_selftest": (ctypes.c_int, [c_int_p]),
     "sph_learned_gemm_check": (ctypes.c_int, [c_float_p, c_float_p, c_float_p, ctypes.c_int,
                                               ctypes.c_int, ctypes.c_int]),
     "sph_cuda_set_learned": (ctypes.c_int, [_P, _P, ctypes.c_float]),

@@ -203,4 +203,32 @@ __device__ __forceinline__ void stencil_rows(unsigned key, const int *__restrict
 
 constexpr int kMaskRow = 64;  // candidates per stencil row recorded in a hit mask
 
+// Visits the set bits of a 64-bit row mask in increasing order with one
+// neighbour's data in flight: load(j) for slot base + t of the next bit is
+// issued before visit(j, data) runs on the previous one, so the loads of a
+// particle's neighbours overlap its arithmetic.  The visiting order is the
+// bits' order.
+template <class T, class Load, class Visit>
+__device__ __forceinline__ void walk_mask(unsigned long long m, int base, Load load, Visit visit)
+{
+    unsigned half[2] = {(unsigned)m, (unsigned)(m >> 32)};
+    bool have = false;
+    int jp = 0;
+    T dp{};
+#pragma unroll
+    for (int hh = 0; hh < 2; ++hh) {
+        unsigned b = half[hh];
+        while (b) {
+            const int j = base + 32 * hh + __ffs(b) - 1;
+            b &= b - 1u;
+            const T d = load(j);
+            if (have) visit(jp, dp);
+            jp = j;
+            dp = d;
+            have = true;
+        }
+    }
+    if (have) visit(jp, dp);
+}
+
 }  // namespace sph

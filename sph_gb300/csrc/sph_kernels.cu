@@ -306,12 +306,12 @@ __device__ __forceinline__ void viscosity_predict_one(
     // One pair's impulse on this particle; self (and any coincident
     // particle) has r2 == 0 and gives none, as u is NaN in the reference for
     // r == 0 (fluid.c:446-451).
-    auto impulse = [&](int j) {
-        const float2 q = __ldg(pos + j);
+    auto impulse_with = [&](const float4 &d) {
+        const float2 q = make_float2(d.x, d.y);
         const float qx = q.x - p.x, qy = q.y - p.y;
         const float r2 = dist2(qx, qy);
         if (r2 > h2 || r2 == 0.0f) return;
-        float2 w = __ldg(vel + j);
+        float2 w = make_float2(d.z, d.w);
         w.y = __fadd_rn(w.y, gdt);
         const float r_recip = rsqrtf(r2);
         const float r = r2 * r_recip;
@@ -323,6 +323,11 @@ __device__ __forceinline__ void viscosity_predict_one(
             dvy -= 0.5f * clamp5(imp * qy * r_recip);
         }
     };
+    auto load_pv = [&](int j) {
+        const float2 q = __ldg(pos + j), w = __ldg(vel + j);
+        return make_float4(q.x, q.y, w.x, w.y);
+    };
+    auto impulse = [&](int j) { impulse_with(load_pv(j)); };
     if ((PROBE || st->lists_valid) && searchable(key, i, start, g, capped, c.max_bucket)) {
         bool walked = false;
         if (!capped) {
@@ -348,14 +353,9 @@ __device__ __forceinline__ void viscosity_predict_one(
                 }
                 m[1] &= ~(1ull << (i - ra[1]));  // self
 #pragma unroll
-                for (int r = 0; r < 3; ++r) {
-                    unsigned long long mr = m[r];
-                    while (mr) {
-                        const int t = __ffsll((long long)mr) - 1;
-                        mr &= mr - 1ull;
-                        impulse(ra[r] + t);
-                    }
-                }
+                for (int r = 0; r < 3; ++r)
+                    walk_mask<float4>(m[r], ra[r], load_pv,
+                                      [&](int, const float4 &d) { impulse_with(d); });
                 walked = true;
             }
         }
@@ -628,15 +628,12 @@ __device__ __forceinline__ void relax_update_one(
                 const ulonglong2 m01 = mask01[i];
                 const unsigned long long mm[3] = {m01.x, m01.y, mask2[i]};
 #pragma unroll
-                for (int r = 0; r < 3; ++r) {
-                    unsigned long long m = mm[r];
-                    while (m) {
-                        const int t = __ffsll((long long)m) - 1;
-                        m &= m - 1ull;
-                        const int j = ra[r] + t;
-                        relax_pair(c, p, Pi, Pni, __ldg(xr + j), i, j, key, ids, g, ax, ay, nudges);
-                    }
-                }
+                for (int r = 0; r < 3; ++r)
+                    walk_mask<float4>(
+                        mm[r], ra[r], [&](int j) { return __ldg(xr + j); },
+                        [&](int j, const float4 &q) {
+                            relax_pair(c, p, Pi, Pni, q, i, j, key, ids, g, ax, ay, nudges);
+                        });
                 walked = true;
             }
         }

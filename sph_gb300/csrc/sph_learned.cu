@@ -737,6 +737,21 @@ __global__ void k_err_targets(Ctx c, const float *__restrict__ rho_net,
     T[r] = t;
 }
 
+// Self-test of the bounded tensor-core wait: waits on an mbarrier that no
+// operation arrives at; the wait gives up after its poll limit and the
+// kernel records that (*gave_up = 1) instead of hanging.
+__global__ void k_wait_selftest(unsigned *__restrict__ gave_up)
+{
+    __shared__ uint64_t mbar;
+    if (threadIdx.x == 0) {
+        tc::mbar_init(&mbar, 1);
+        tc::mbar_fence_init();
+    }
+    __syncthreads();
+    const bool done = tc::mbar_wait(&mbar, 0);
+    if (threadIdx.x == 0) *gave_up = done ? 0u : 1u;
+}
+
 }  // namespace ml
 
 // The learned-relaxation model.
@@ -1050,6 +1065,26 @@ using namespace sph;
 extern "C" {
 
 int sph_learned_num_params(void) { return ml::NPARAM; }
+
+int sph_learned_wait_selftest(int *gave_up)
+{
+    if (!gave_up) {
+        set_error("null argument");
+        return SPH_ERR_INVALID;
+    }
+    unsigned *d = nullptr;
+    LCUDA(cudaMalloc(&d, sizeof(unsigned)));
+    int rc = cuda_fail(cudaMemset(d, 0xFF, sizeof(unsigned)), "memset");
+    if (!rc) {
+        ml::k_wait_selftest<<<1, 32>>>(d);
+        rc = cuda_fail(cudaGetLastError(), "selftest launch");
+    }
+    unsigned h = 0xFFFFFFFFu;
+    if (!rc) rc = cuda_fail(cudaMemcpy(&h, d, sizeof(h), cudaMemcpyDeviceToHost), "selftest");
+    cudaFree(d);
+    if (!rc) *gave_up = (int)h;
+    return rc;
+}
 
 int sph_learned_create(sph_learned_t **out, int max_samples, unsigned long long seed)
 {

@@ -117,11 +117,21 @@ __device__ __forceinline__ void mbar_fence_init()
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
+__device__ __forceinline__ uint64_t globaltimer_ns()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 // Waits for phase `parity` of the mbarrier to complete; gives up after
-// kSpinLimit polls and returns false (the caller records an error).
+// kWaitNs nanoseconds of the GPU's global timer (or kSpinLimit polls) and
+// returns false (the caller records an error).
+constexpr uint64_t kWaitNs = 1000000000ull;  // 1 s: any tensor-core step takes microseconds
 __device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity)
 {
     const uint32_t a = smem_u32(mbar);
+    const uint64_t t0 = globaltimer_ns();
     for (uint32_t it = 0; it < kSpinLimit; ++it) {
         uint32_t done;
         asm volatile(
@@ -130,6 +140,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity)
             "selp.u32 %0, 1, 0, p;\n\t}"
             : "=r"(done) : "r"(a), "r"(parity) : "memory");
         if (done) return true;
+        if (globaltimer_ns() - t0 > kWaitNs) return false;
     }
     return false;
 }

@@ -268,3 +268,16 @@ def test_skewed_ensemble_learned(trained):
     finally:
         a.close()
         b.close()
+
+
+def test_bounded_wait_gives_up(cuda_lib):
+    """A tensor-core wait on an mbarrier that nothing arrives at ends with a
+    recorded error status (no hang), and the context stays usable."""
+    import ctypes
+    from sph_gb300 import _lib
+    flag = ctypes.c_int(-1)
+    _lib.check(cuda_lib.sph_learned_wait_selftest(ctypes.byref(flag)))
+    assert flag.value == 1
+    # the device still works afterwards
+    A = np.ones((128, 32), np.float32)
+    assert np.allclose(gemm_check(A, A[:16]), 32.0)
