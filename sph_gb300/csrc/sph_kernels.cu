@@ -340,16 +340,25 @@ __device__ __forceinline__ void viscosity_predict_one(
 #pragma unroll
                 for (int r = 0; r < 3; ++r) {
                     const float2 *row = pos + ra[r];
-                    unsigned long long mr = 0ull;
+                    const int len = rl[r];
+                    // 32-bit halves: cheaper bit operations than one 64-bit mask
+                    unsigned lo = 0u, hi = 0u;
+                    const int n0 = min(len, 32);
 #pragma unroll 4
-                    for (int t = 0; t < rl[r]; ++t) {
+                    for (int t = 0; t < n0; ++t) {
                         const float2 q = __ldg(row + t);
                         const float r2 = dist2(q.x - p.x, q.y - p.y);
                         // self and coincident particles are marked too; the
                         // impulse skips them (r2 == 0)
-                        mr |= (unsigned long long)(r2 <= h2) << t;
+                        lo |= (unsigned)(r2 <= h2) << t;
                     }
-                    m[r] = mr;
+#pragma unroll 4
+                    for (int t = 32; t < len; ++t) {
+                        const float2 q = __ldg(row + t);
+                        const float r2 = dist2(q.x - p.x, q.y - p.y);
+                        hi |= (unsigned)(r2 <= h2) << (t - 32);
+                    }
+                    m[r] = ((unsigned long long)hi << 32) | lo;
                 }
                 m[1] &= ~(1ull << (i - ra[1]));  // self
 #pragma unroll
@@ -432,13 +441,34 @@ __device__ __forceinline__ void density_one(int i, const Ctx &c, const float2 *_
 #pragma unroll
             for (int r = 0; r < 3; ++r) {
                 const float2 *row = pos + ra[r];
-                unsigned long long mr = 0ull;
+                const int len = rl[r];
+                unsigned mh[2] = {0u, 0u};  // 32-bit halves of the row's hit mask
+#pragma unroll
+                for (int hh = 0; hh < 2; ++hh) {
+                    const int t1 = hh == 0 ? min(len, 32) : min(len, kMaskRow);
 #pragma unroll 4
-                for (int t = 0; t < rl[r]; ++t) {
+                    for (int t = 32 * hh; t < t1; ++t) {
+                        const float2 q = __ldg(row + t);
+                        const float r2 = dist2(p.x - q.x, p.y - q.y);
+                        if (r2 <= h2) {
+                            mh[hh] |= 1u << (t & 31);
+                            const float rr = r2 > 0.0f ? r2 * rsqrtf(r2) : 0.0f;
+                            const float ratio = __fmul_rn(rr, h_recip);
+                            if (ratio < 1.0f) {
+                                const float omr = 1.0f - ratio;
+                                const float omr2 = omr * omr;
+                                a += omr2;
+                                b += omr2 * omr;
+                            }
+                        }
+                    }
+                }
+                // rows longer than the mask (the relaxation then walks the
+                // whole stencil): the remaining candidates, no mask bits
+                for (int t = kMaskRow; t < len; ++t) {
                     const float2 q = __ldg(row + t);
                     const float r2 = dist2(p.x - q.x, p.y - q.y);
                     if (r2 <= h2) {
-                        mr |= 1ull << (t & 63);
                         const float rr = r2 > 0.0f ? r2 * rsqrtf(r2) : 0.0f;
                         const float ratio = __fmul_rn(rr, h_recip);
                         if (ratio < 1.0f) {
@@ -449,7 +479,7 @@ __device__ __forceinline__ void density_one(int i, const Ctx &c, const float2 *_
                         }
                     }
                 }
-                m[r] = mr;
+                m[r] = ((unsigned long long)mh[1] << 32) | mh[0];
             }
             // the particle met itself (r = 0) in its own row: remove it
             a -= 1.0f;
