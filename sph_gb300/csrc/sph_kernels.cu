@@ -558,18 +558,32 @@ struct RelaxConsts {
     float h2, hh, h_recip, dt2, k, k_near, rest, half_spring;
 };
 
-// One neighbour's contribution to the displacement (r2 <= h2 known).
-__device__ __forceinline__ void relax_pair(const RelaxConsts &c, float2 p, float Pi, float Pni,
-                                           float4 q, int i, int j, unsigned key,
-                                           const int *__restrict__ ids, const SG &g, float &ax,
-                                           float &ay, int &nudges)
+// One neighbour's contribution to the displacement (r2 <= h2 known), with
+// the constants pre-multiplied by dt^2; the rare r <= 1e-6 path computes
+// the grid and cell key it needs itself, so that they are not live across
+// the neighbour walk.
+struct WalkConsts {
+    float h_recip, kd, knd, hsd, hshd, Pd, Pnd;
+};
+
+__device__ __noinline__ bool owns_pair_of(const Scene *S, float2 p, const int *__restrict__ ids,
+                                          int i, float2 q, int j)
+{
+    const SG g = load_grid(S);
+    return owns_pair(cell_key(p.x, p.y, g), ids[i], q, ids[j], g);
+}
+
+__device__ __forceinline__ void relax_pair_walk(const WalkConsts &c, float2 p, float4 q, int i,
+                                                int j, const Scene *S,
+                                                const int *__restrict__ ids, float &ax,
+                                                float &ay, int &nudges)
 {
     const float ex = p.x - q.x, ey = p.y - q.y;
     const float r2 = dist2(ex, ey);
     if (r2 <= 2e-12f) {
         // r <= 1e-6 (rare): the owner of the pair is nudged (fluid.c:583-586)
         const float r = r2 > 0.0f ? __fsqrt_rn(r2) : 0.0f;
-        if (j != i && r <= 0.000001f && owns_pair(key, ids[i], make_float2(q.x, q.y), ids[j], g))
+        if (j != i && r <= 0.000001f && owns_pair_of(S, p, ids, i, make_float2(q.x, q.y), j))
             ++nudges;
         if (!(r > 0.0f)) return;
     }
@@ -578,8 +592,8 @@ __device__ __forceinline__ void relax_pair(const RelaxConsts &c, float2 p, float
     const float ratio = r * c.h_recip;
     if (ratio < 1.0f) {
         const float omr = 1.0f - ratio;
-        const float D = c.dt2 * ((Pi + c.k * (q.z - c.rest)) * omr +
-                                 (Pni + c.k_near * q.w) * omr * omr + c.half_spring * (c.hh - r));
+        const float D = (c.Pd + c.kd * q.z) * omr + (c.Pnd + c.knd * q.w) * omr * omr +
+                        (c.hshd - c.hsd * r);
         const float s = D * r_recip;
         ax += s * ex;
         ay += s * ey;
@@ -635,6 +649,15 @@ __device__ __forceinline__ void relax_update_one(
     const float2 p = make_float2(me.x, me.y);
     const float Pi = c.k * (me.z - c.rest), Pni = c.k_near * me.w;
     const unsigned key = cell_key(p.x, p.y, g);
+    // constants of the masked walk, pre-multiplied by dt^2 (fewer live values)
+    WalkConsts wc;
+    wc.h_recip = c.h_recip;
+    wc.kd = c.dt2 * c.k;
+    wc.knd = c.dt2 * c.k_near;
+    wc.hsd = c.dt2 * c.half_spring;
+    wc.hshd = wc.hsd * c.hh;
+    wc.Pd = c.dt2 * (Pi - c.k * c.rest);
+    wc.Pnd = c.dt2 * Pni;
     float ax = 0.0f, ay = 0.0f;
     int nudges = 0;
     bool net = false;
@@ -662,7 +685,7 @@ __device__ __forceinline__ void relax_update_one(
                     walk_mask<float4>(
                         mm[r], ra[r], [&](int j) { return __ldg(xr + j); },
                         [&](int j, const float4 &q) {
-                            relax_pair(c, p, Pi, Pni, q, i, j, key, ids, g, ax, ay, nudges);
+                            relax_pair_walk(wc, p, q, i, j, S, ids, ax, ay, nudges);
                         });
                 walked = true;
             }
@@ -672,7 +695,7 @@ __device__ __forceinline__ void relax_update_one(
                 if (j == i) return;
                 const float4 q = __ldg(xr + j);
                 if (dist2(p.x - q.x, p.y - q.y) > c.h2) return;
-                relax_pair(c, p, Pi, Pni, q, i, j, key, ids, g, ax, ay, nudges);
+                relax_pair_walk(wc, p, q, i, j, S, ids, ax, ay, nudges);
             });
         }
     }
@@ -685,9 +708,10 @@ __device__ __forceinline__ void relax_update_one(
     float ny = __fadd_rn(__fadd_rn(p.y, ay), nd);
     boundary_of(nx, ny, S);
     const float2 pv = prev[i];
-    const float vx = clamp5(__fdiv_rn(__fsub_rn(nx, pv.x), dt));
-    const float vy = clamp5(__fdiv_rn(__fsub_rn(ny, pv.y), dt));
-    const unsigned k2 = cell_key(nx, ny, g);
+    const float dt_end = __ldg(&S->P.time_step);
+    const float vx = clamp5(__fdiv_rn(__fsub_rn(nx, pv.x), dt_end));
+    const float vy = clamp5(__fdiv_rn(__fsub_rn(ny, pv.y), dt_end));
+    const unsigned k2 = cell_key(nx, ny, load_grid(S));
     const unsigned rank = atomicAdd(cnt + k2, 1u);
     pos_out[i] = make_float2(nx, ny);
     vel_out[i] = make_float2(vx, vy);
