@@ -298,9 +298,8 @@ class DamBreak:
     def step_one(self, sim, t):
         sim.step(self.p(t))
 
-    def tune(self, sim, t0):
-        shapes = sim.autotune(1)  # 8 steps with the tunables of step t0 - 1
-        return t0 + 8, shapes
+    def tune(self, sim):
+        return sim.autotune(1)  # 48 steps with the tunables of the last step
 
     def cpu_sample(self, args):
         return cpu_baseline_single(args.cpu_sample, args.cpu_steps)
@@ -329,9 +328,8 @@ class EnsembleWork:
     def step_one(self, sim, t):
         sim.step(None, 1)
 
-    def tune(self, sim, t0):
-        shapes = sim.autotune(2)  # 16 steps, part of the warm-up
-        return t0 + 16, shapes
+    def tune(self, sim):
+        return sim.autotune(2)  # 96 steps (2 interleaved rounds)
 
     def cpu_sample(self, args):
         import oracle
@@ -388,7 +386,7 @@ def train_learned(args):
     return m, info
 
 
-def run_learned(args, work, plain_ms):
+def run_learned(args, work, plain_ms, shapes):
     """The learned step on the dam break: throughput (CUDA events around
     graph-launched steps), one-step RMS density error against the plain step
     from the same state, the fallback share, and a 1,000-step trajectory's
@@ -398,6 +396,7 @@ def run_learned(args, work, plain_ms):
     thr = args.learned_threshold
     K, W = args.steps, args.warmup
     sim = work.fresh()
+    sim.set_launch_shapes(shapes)
     work.advance(sim, 0, W)
     sim.set_learned(model, thr)
     work.advance(sim, W, 5)
@@ -480,9 +479,13 @@ def run_skewed(args, world, rank):
 
     res = {}
     for label in ("plain", "learned"):
+        tuner = fresh(label == "learned")  # shapes tuned on a copy at step W
+        tuner.step(None, W)
+        shapes = tuner.autotune(1)
+        tuner.close()
         e = fresh(label == "learned")
+        e.set_launch_shapes(shapes)
         e.step(None, W)
-        shapes = e.autotune(2)
         e.synchronize()
         barrier(world)
         with ClockSampler(0) as clk:
@@ -558,10 +561,18 @@ def run_gpu(args, world, rank):
     n, cells = work.n, work.cells
     K, W = args.steps, args.warmup
 
+    # ---- launch shapes: tuned on a copy of the scene at step W, so that the
+    # timed steps are steps W .. W+K-1 of the run ----
+    tuner = work.fresh()
+    work.advance(tuner, 0, W)
+    shapes = work.tune(tuner)
+    tuner.close()
+
     # ---- device-resident throughput ----
     sim = work.fresh()
+    sim.set_launch_shapes(shapes)
     work.advance(sim, 0, W)
-    t0, shapes = work.tune(sim, W)
+    t0 = W
     sim.synchronize()
     barrier(world)
     with ClockSampler(0) as clk:
@@ -602,6 +613,7 @@ def run_gpu(args, world, rank):
         coords = [PinnedArray((n, 2), np.int16) for _ in range(2)]
         tw = time.perf_counter()
         sim2 = work.fresh()
+        sim2.set_launch_shapes(shapes)
         for t in range(W + K):
             work.step_one(sim2, t)
             sim2.pack_coords_async(coords[t % 2].array)
@@ -626,7 +638,7 @@ def run_gpu(args, world, rank):
     learned = None
     if args.workload == "dam_break" and not args.no_learned:
         try:
-            learned = run_learned(args, work, ms / K)
+            learned = run_learned(args, work, ms / K, shapes)
         except Exception as exc:  # reported, never hidden
             learned = {"error": f"{type(exc).__name__}: {exc}"}
 

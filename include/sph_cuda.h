@@ -141,9 +141,12 @@ int sph_cuda_scene_diagnostics(sph_cuda_t *h, double *out);
 int sph_cuda_set_launch_shapes(sph_cuda_t *h, const int *shapes);
 int sph_cuda_get_launch_shapes(sph_cuda_t *h, int *shapes);
 
-/* Autotuner: times every candidate shape on the three gathers for
- * trial_steps steps each (the steps advance the simulation) and keeps the
- * fastest per gather; the chosen shapes go to shapes_out (6 ints) if given. */
+/* Autotuner: for each gather in turn (the others at their best so far),
+ * times one graph-launched step per candidate shape over trial_steps
+ * interleaved rounds and keeps the candidate with the lowest median step
+ * time.  It advances the simulation by 48 x trial_steps steps (each
+ * measurement re-captures the step graph with one untimed step first); the
+ * chosen shapes go to shapes_out (6 ints) if given. */
 int sph_cuda_autotune(sph_cuda_t *h, int trial_steps, int *shapes_out);
 
 /* Frees all device and host resources of the handle. */

@@ -100,7 +100,9 @@ int sph_learned_wait_selftest(int *gave_up);
 int sph_cuda_set_learned(sph_cuda_t *h, sph_learned_t *l, float threshold);
 
 /* Particle-steps that used the network and that fell back to the plain
- * relaxation, since the model was attached. */
+ * relaxation, since the model was attached.  Returns SPH_ERR_CUDA if a
+ * tensor-core wait of the attached network gave up during those steps
+ * (their results are then not valid). */
 int sph_cuda_learned_counts(sph_cuda_t *h, unsigned long long *learned,
                             unsigned long long *fallback);
 

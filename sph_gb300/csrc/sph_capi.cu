@@ -959,32 +959,41 @@ int sph_cuda_autotune(sph_cuda_t *h, int trial_steps, int *shapes_out)
     static const Shape cands[] = {{128, 0}, {256, 0}, {512, 0}, {256, 2}, {256, 4},
                                   {128, 8}, {512, 1}, {512, 2}};
     const int nc = (int)(sizeof(cands) / sizeof(cands[0]));
-    float best[kGathers];
+    // What is measured is what runs: one graph-launched step per candidate,
+    // CUDA events around it.  One gather at a time (coordinate descent, the
+    // others at their best so far); the candidates of a gather are
+    // interleaved, one step each per round, so that the state's drift (the
+    // gathers slow down as a scene compresses) reaches all of them alike;
+    // the lowest median wins.
     Shape pick[kGathers];
+    for (int k = 0; k < kGathers; ++k) pick[k] = h->shape[k];
     for (int k = 0; k < kGathers; ++k) {
-        best[k] = 3.4e38f;
-        pick[k] = h->shape[k];
-    }
-    const int gather_idx[kGathers] = {0, 5, 6};  // positions in the step's kernel order
-    for (int c = 0; c < nc; ++c) {
-        for (int k = 0; k < kGathers; ++k) {
-            Shape s = cands[c];
-            if (k == 2 && s.block > kBlock) s.block = kBlock;
-            h->shape[k] = s;
-        }
-        std::vector<float> t[kGathers];
-        for (int r = 0; r < trial_steps; ++r) {
-            float ms[kMaxKernelsPerStep];
-            int cnt = 0;
-            SPH_TRY(sph_cuda_kernel_times(h, nullptr, ms, kMaxKernelsPerStep, &cnt));
-            for (int k = 0; k < kGathers; ++k) t[k].push_back(ms[gather_idx[k]]);
-        }
-        for (int k = 0; k < kGathers; ++k) {
-            std::sort(t[k].begin(), t[k].end());
-            const float med = t[k][t[k].size() / 2];
-            if (med < best[k]) {
-                best[k] = med;
-                pick[k] = h->shape[k];
+        std::vector<float> t[sizeof(cands) / sizeof(cands[0])];
+        for (int r = 0; r < trial_steps; ++r)
+            for (int c = 0; c < nc; ++c) {
+                Shape sc = cands[c];
+                if (k == 2 && sc.block > kBlock) sc.block = kBlock;  // relax_update: <= 256
+                for (int q = 0; q < kGathers; ++q) h->shape[q] = pick[q];
+                h->shape[k] = sc;
+                destroy_graph(h);
+                SPH_TRY(run_steps(h, 1));  // captures the graph with these shapes
+                SPH_CUDA(cudaEventRecord(h->timer[0], h->stream));
+                SPH_TRY(run_steps(h, 1));
+                SPH_CUDA(cudaEventRecord(h->timer[1], h->stream));
+                SPH_CUDA(cudaEventSynchronize(h->timer[1]));
+                float ms = 0.0f;
+                SPH_CUDA(cudaEventElapsedTime(&ms, h->timer[0], h->timer[1]));
+                t[c].push_back(ms);
+            }
+        float best = 3.4e38f;
+        for (int c = 0; c < nc; ++c) {
+            std::sort(t[c].begin(), t[c].end());
+            const float med = t[c][t[c].size() / 2];
+            if (med < best) {
+                best = med;
+                Shape sc = cands[c];
+                if (k == 2 && sc.block > kBlock) sc.block = kBlock;
+                pick[k] = sc;
             }
         }
     }

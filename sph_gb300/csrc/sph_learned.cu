@@ -1416,8 +1416,9 @@ int sph_learned_calibrate(sph_learned_t *l, sph_cuda_t *h, int epochs, float lr,
         h->learned_thr = thr;
         if (rc) break;
         // network displacement of the same state
-        LCUDA(cudaMemsetAsync(l->d_err, 0, 4, h->stream));
-        LCUDA(cudaStreamSynchronize(l->stream));
+        if ((rc = cuda_fail(cudaMemsetAsync(l->d_err, 0, 4, h->stream), "memset")) ||
+            (rc = cuda_fail(cudaStreamSynchronize(l->stream), "sync")))
+            break;
         if ((rc = run_mlp(h->stream, l, n, (const __nv_bfloat16 *)h->feat_c, h->net_c, h->num_sms)))
             break;
         const Ctx c = make_ctx(h);
@@ -1478,6 +1479,17 @@ int sph_cuda_learned_counts(sph_cuda_t *h, unsigned long long *learned, unsigned
     LCUDA(cudaMemcpyAsync(v, &h->d_state->learned_steps, sizeof(v), cudaMemcpyDeviceToHost,
                           h->stream));
     LCUDA(cudaStreamSynchronize(h->stream));
+    if (h->learned) {
+        // a tensor-core wait that gave up inside a step leaves its tiles'
+        // outputs unwritten: report it here rather than hide it
+        unsigned e = 0;
+        LCUDA(cudaMemcpy(&e, h->learned->d_err, sizeof(e), cudaMemcpyDeviceToHost));
+        if (e) {
+            set_error("the network kernel's tensor-core wait gave up %u times: results of "
+                      "the learned steps are not valid", e);
+            return SPH_ERR_CUDA;
+        }
+    }
     const unsigned long long total = v[0] * (unsigned long long)h->n;
     *fallback = v[1];
     *learned = total >= v[1] ? total - v[1] : 0ull;

@@ -140,8 +140,9 @@ class Simulation:
         check(lib().sph_cuda_set_scene_params(self._h, int(scene), ctypes.byref(tunables(params))))
 
     def autotune(self, trial_steps: int = 3) -> list:
-        """Picks the fastest launch shape per gather kernel (advances the
-        simulation by 8 * trial_steps steps); returns the 6 shape ints."""
+        """Picks the fastest launch shape per gather kernel by timing
+        graph-launched steps (advances the simulation by 48 * trial_steps
+        steps); returns the 6 shape ints."""
         out = (ctypes.c_int * 6)()
         check(lib().sph_cuda_autotune(self._h, int(trial_steps), out))
         return list(out)

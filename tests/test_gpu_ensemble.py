@@ -29,7 +29,7 @@ def run_ensemble(scs, steps, shapes=None, autotune=False):
     if shapes is not None:
         e.set_launch_shapes(shapes)
     if autotune:
-        chosen = e.autotune(1)  # advances 8 steps
+        chosen = e.autotune(1)  # advances 48 steps
         # re-upload so every run starts from the same state
         e.upload_scenes()
         assert chosen == e.launch_shapes()
