@@ -132,6 +132,17 @@ __device__ __forceinline__ float dist2(float dx, float dy)
     return __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
 }
 
+// dist2 of p and q in packed FP32x2 arithmetic (sm_100+): d = q - p per
+// component (given mp = -p), r2 = d.x^2 + d.y^2, each operation rounded
+// exactly as dist2(p.x - q.x, p.y - q.y) rounds it (the squares of +-dx
+// are equal), in three instructions instead of five.
+__device__ __forceinline__ float dist2_packed(float2 mp, float2 q, float2 &d)
+{
+    d = __fadd2_rn(q, mp);
+    const float2 s = __fmul2_rn(d, d);
+    return __fadd_rn(s.x, s.y);
+}
+
 // Visits the candidate slots of the 3x3 cell stencil around `key` in sorted
 // order.  Without bucket overflow, the three cells of a stencil row are
 // contiguous in the sorted arrays, so each row is one range

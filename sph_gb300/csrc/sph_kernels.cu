@@ -306,10 +306,11 @@ __device__ __forceinline__ void viscosity_predict_one(
     // One pair's impulse on this particle; self (and any coincident
     // particle) has r2 == 0 and gives none, as u is NaN in the reference for
     // r == 0 (fluid.c:446-451).
+    const float2 mp = make_float2(-p.x, -p.y);
     auto impulse_with = [&](const float4 &d) {
-        const float2 q = make_float2(d.x, d.y);
-        const float qx = q.x - p.x, qy = q.y - p.y;
-        const float r2 = dist2(qx, qy);
+        float2 e;
+        const float r2 = dist2_packed(mp, make_float2(d.x, d.y), e);
+        const float qx = e.x, qy = e.y;
         if (r2 > h2 || r2 == 0.0f) return;
         float2 w = make_float2(d.z, d.w);
         w.y = __fadd_rn(w.y, gdt);
@@ -346,16 +347,16 @@ __device__ __forceinline__ void viscosity_predict_one(
                     const int n0 = min(len, 32);
 #pragma unroll 4
                     for (int t = 0; t < n0; ++t) {
-                        const float2 q = __ldg(row + t);
-                        const float r2 = dist2(q.x - p.x, q.y - p.y);
+                        float2 e;
+                        const float r2 = dist2_packed(mp, __ldg(row + t), e);
                         // self and coincident particles are marked too; the
                         // impulse skips them (r2 == 0)
                         lo |= (unsigned)(r2 <= h2) << t;
                     }
 #pragma unroll 4
                     for (int t = 32; t < len; ++t) {
-                        const float2 q = __ldg(row + t);
-                        const float r2 = dist2(q.x - p.x, q.y - p.y);
+                        float2 e;
+                        const float r2 = dist2_packed(mp, __ldg(row + t), e);
                         hi |= (unsigned)(r2 <= h2) << (t - 32);
                     }
                     m[r] = ((unsigned long long)hi << 32) | lo;
@@ -431,6 +432,7 @@ __device__ __forceinline__ void density_one(int i, const Ctx &c, const float2 *_
     const float h2 = __fmul_rn(hh, hh);
     const float h_recip = __fdiv_rn(1.0f, hh);
     const float2 p = pos[i];
+    const float2 mp = make_float2(-p.x, -p.y);
     const unsigned key = cell_key(p.x, p.y, g);
     float a = 0.0f, b = 0.0f;
     unsigned long long m[3] = {0ull, 0ull, 0ull};
@@ -448,8 +450,8 @@ __device__ __forceinline__ void density_one(int i, const Ctx &c, const float2 *_
                     const int t1 = hh == 0 ? min(len, 32) : min(len, kMaskRow);
 #pragma unroll 4
                     for (int t = 32 * hh; t < t1; ++t) {
-                        const float2 q = __ldg(row + t);
-                        const float r2 = dist2(p.x - q.x, p.y - q.y);
+                        float2 e;
+                        const float r2 = dist2_packed(mp, __ldg(row + t), e);
                         if (r2 <= h2) {
                             mh[hh] |= 1u << (t & 31);
                             const float rr = r2 > 0.0f ? r2 * rsqrtf(r2) : 0.0f;
@@ -466,8 +468,8 @@ __device__ __forceinline__ void density_one(int i, const Ctx &c, const float2 *_
                 // rows longer than the mask (the relaxation then walks the
                 // whole stencil): the remaining candidates, no mask bits
                 for (int t = kMaskRow; t < len; ++t) {
-                    const float2 q = __ldg(row + t);
-                    const float r2 = dist2(p.x - q.x, p.y - q.y);
+                    float2 e;
+                    const float r2 = dist2_packed(mp, __ldg(row + t), e);
                     if (r2 <= h2) {
                         const float rr = r2 > 0.0f ? r2 * rsqrtf(r2) : 0.0f;
                         const float ratio = __fmul_rn(rr, h_recip);
@@ -578,8 +580,8 @@ __device__ __forceinline__ void relax_pair_walk(const WalkConsts &c, float2 p, f
                                                 const int *__restrict__ ids, float &ax,
                                                 float &ay, int &nudges)
 {
-    const float ex = p.x - q.x, ey = p.y - q.y;
-    const float r2 = dist2(ex, ey);
+    float2 d;  // q - p: the negated pair offset, rounded as p - q is
+    const float r2 = dist2_packed(make_float2(-p.x, -p.y), make_float2(q.x, q.y), d);
     if (r2 <= 2e-12f) {
         // r <= 1e-6 (rare): the owner of the pair is nudged (fluid.c:583-586)
         const float r = r2 > 0.0f ? __fsqrt_rn(r2) : 0.0f;
@@ -595,8 +597,8 @@ __device__ __forceinline__ void relax_pair_walk(const WalkConsts &c, float2 p, f
         const float D = (c.Pd + c.kd * q.z) * omr + (c.Pnd + c.knd * q.w) * omr * omr +
                         (c.hshd - c.hsd * r);
         const float s = D * r_recip;
-        ax += s * ex;
-        ay += s * ey;
+        ax -= s * d.x;  // += s (p - q)
+        ay -= s * d.y;
     }
 }
 

@@ -100,6 +100,7 @@ k_features(Ctx c, const float2 *__restrict__ pos, const float2 *__restrict__ pre
     const float2 p = pos[i];
     const float2 pp = prev[i];
     const float vix = (p.x - pp.x) * inv_dt, viy = (p.y - pp.y) * inv_dt;
+    const float2 mp = make_float2(-p.x, -p.y);
     const unsigned key = cell_key(p.x, p.y, g);
     float a = 0.0f, b = 0.0f;
     unsigned long long m[3] = {0ull, 0ull, 0ull};
@@ -117,8 +118,9 @@ k_features(Ctx c, const float2 *__restrict__ pos, const float2 *__restrict__ pre
                 unsigned long long mr = 0ull;
                 for (int t = 0; t < rl[r]; ++t) {
                     const float2 q = __ldg(row + t);
-                    const float ex = q.x - p.x, ey = q.y - p.y;
-                    const float r2 = dist2(p.x - q.x, p.y - q.y);
+                    float2 e;  // q - p
+                    const float r2 = dist2_packed(mp, q, e);
+                    const float ex = e.x, ey = e.y;
                     if (r2 <= h2) {
                         mr |= 1ull << (t & 63);
                         const float rinv = rsqrtf(r2);
