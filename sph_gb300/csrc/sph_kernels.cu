@@ -301,7 +301,7 @@ __device__ __forceinline__ void viscosity_predict_one(
     const float2 p = pos[i];
     float2 v = vel[i];
     v.y = __fadd_rn(v.y, gdt);
-    float dvx = 0.0f, dvy = 0.0f;
+    float2 dv = make_float2(0.0f, 0.0f);
     const unsigned key = cell_key(p.x, p.y, g);
     // One pair's impulse on this particle; self (and any coincident
     // particle) has r2 == 0 and gives none, as u is NaN in the reference for
@@ -320,8 +320,11 @@ __device__ __forceinline__ void viscosity_predict_one(
         if (u > 0.0f) {
             const float ratio = r * h_recip;
             const float imp = dt * (1.0f - ratio) * (sigma * u + beta * u * u);
-            dvx -= 0.5f * clamp5(imp * qx * r_recip);
-            dvy -= 0.5f * clamp5(imp * qy * r_recip);
+            // per component imp * q * r_recip, clamped, halved and subtracted
+            // (packed FP32x2, each operation rounded as the scalar form)
+            const float2 t = __fmul2_rn(__fmul2_rn(make_float2(imp, imp), e),
+                                        make_float2(r_recip, r_recip));
+            dv = __ffma2_rn(make_float2(-0.5f, -0.5f), make_float2(clamp5(t.x), clamp5(t.y)), dv);
         }
     };
     auto load_pv = [&](int j) {
@@ -372,11 +375,11 @@ __device__ __forceinline__ void viscosity_predict_one(
         if (!walked) for_each_candidate(key, start, g, capped, c.max_bucket, impulse);
     }
     if (PROBE) {
-        probe_out[i] = make_float2(dvx, dvy);
+        probe_out[i] = dv;
         return;
     }
-    v.x = __fadd_rn(v.x, dvx);
-    v.y = __fadd_rn(v.y, dvy);
+    v.x = __fadd_rn(v.x, dv.x);
+    v.y = __fadd_rn(v.y, dv.y);
     float nx = __fadd_rn(p.x, __fmul_rn(v.x, dt));
     float ny = __fadd_rn(p.y, __fmul_rn(v.y, dt));
     boundary_of(nx, ny, S);
@@ -577,8 +580,8 @@ __device__ __noinline__ bool owns_pair_of(const Scene *S, float2 p, const int *_
 
 __device__ __forceinline__ void relax_pair_walk(const WalkConsts &c, float2 p, float4 q, int i,
                                                 int j, const Scene *S,
-                                                const int *__restrict__ ids, float &ax,
-                                                float &ay, int &nudges)
+                                                const int *__restrict__ ids, float2 &a,
+                                                int &nudges)
 {
     float2 d;  // q - p: the negated pair offset, rounded as p - q is
     const float r2 = dist2_packed(make_float2(-p.x, -p.y), make_float2(q.x, q.y), d);
@@ -597,8 +600,7 @@ __device__ __forceinline__ void relax_pair_walk(const WalkConsts &c, float2 p, f
         const float D = (c.Pd + c.kd * q.z) * omr + (c.Pnd + c.knd * q.w) * omr * omr +
                         (c.hshd - c.hsd * r);
         const float s = D * r_recip;
-        ax -= s * d.x;  // += s (p - q)
-        ay -= s * d.y;
+        a = __ffma2_rn(make_float2(-s, -s), d, a);  // += s (p - q), per component
     }
 }
 
@@ -660,15 +662,14 @@ __device__ __forceinline__ void relax_update_one(
     wc.hshd = wc.hsd * c.hh;
     wc.Pd = c.dt2 * (Pi - c.k * c.rest);
     wc.Pnd = c.dt2 * Pni;
-    float ax = 0.0f, ay = 0.0f;
+    float2 acc = make_float2(0.0f, 0.0f);  // the displacement
     int nudges = 0;
     bool net = false;
     if (LEARNED && (int)__ldg(L.nbc + i) <= L.max_nb) {
         const float4 y = __ldg(L.net + i);
         if (y.z <= L.thr_pct) {
             const float s = c.hh * c.dt2 * (c.k + c.k_near + 2.0f * c.half_spring);
-            ax = y.x * s;
-            ay = y.y * s;
+            acc = make_float2(y.x * s, y.y * s);
             net = true;
         }
     }
@@ -687,7 +688,7 @@ __device__ __forceinline__ void relax_update_one(
                     walk_mask<float4>(
                         mm[r], ra[r], [&](int j) { return __ldg(xr + j); },
                         [&](int j, const float4 &q) {
-                            relax_pair_walk(wc, p, q, i, j, S, ids, ax, ay, nudges);
+                            relax_pair_walk(wc, p, q, i, j, S, ids, acc, nudges);
                         });
                 walked = true;
             }
@@ -697,17 +698,17 @@ __device__ __forceinline__ void relax_update_one(
                 if (j == i) return;
                 const float4 q = __ldg(xr + j);
                 if (dist2(p.x - q.x, p.y - q.y) > c.h2) return;
-                relax_pair_walk(wc, p, q, i, j, S, ids, ax, ay, nudges);
+                relax_pair_walk(wc, p, q, i, j, S, ids, acc, nudges);
             });
         }
     }
     const float nd = (float)nudges * 0.000001f;
     if (PROBE) {
-        probe_out[i] = make_float2(ax + nd, ay + nd);
+        probe_out[i] = make_float2(acc.x + nd, acc.y + nd);
         return;
     }
-    float nx = __fadd_rn(__fadd_rn(p.x, ax), nd);
-    float ny = __fadd_rn(__fadd_rn(p.y, ay), nd);
+    float nx = __fadd_rn(__fadd_rn(p.x, acc.x), nd);
+    float ny = __fadd_rn(__fadd_rn(p.y, acc.y), nd);
     boundary_of(nx, ny, S);
     const float2 pv = prev[i];
     const float dt_end = __ldg(&S->P.time_step);
