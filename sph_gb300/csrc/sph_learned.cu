@@ -104,8 +104,8 @@ k_features(Ctx c, const float2 *__restrict__ pos, const float2 *__restrict__ pre
     const unsigned key = cell_key(p.x, p.y, g);
     float a = 0.0f, b = 0.0f;
     unsigned long long m[3] = {0ull, 0ull, 0ull};
-    float V1x = 0.0f, V1y = 0.0f, V2x = 0.0f, V2y = 0.0f, Ms = 0.0f;
-    float Txx = 0.0f, Txy = 0.0f, Tyy = 0.0f, Dx = 0.0f, Dy = 0.0f;
+    float2 V1 = make_float2(0.0f, 0.0f), V2 = V1, Tdiag = V1, Dsum = V1;
+    float Ms = 0.0f, Txy = 0.0f;
     int count = 0;
     bool degenerate = false;
     if (searchable(key, i, start, g, capped, c.max_bucket)) {
@@ -135,19 +135,18 @@ k_features(Ctx c, const float2 *__restrict__ pos, const float2 *__restrict__ pre
                             a += omr2;
                             b += omr2 * omr;
                             if (other) {
-                                const float ux = ex * rinv, uy = ey * rinv;
-                                const float wux = omr * ux, wuy = omr * uy;
-                                V1x += wux;
-                                V1y += wuy;
-                                V2x += omr2 * ux;
-                                V2y += omr2 * uy;
+                                // message sums in packed FP32x2 arithmetic
+                                const float2 u = __fmul2_rn(e, make_float2(rinv, rinv));
+                                const float2 w2 = make_float2(omr, omr);
+                                const float2 wu = __fmul2_rn(w2, u);
+                                V1 = __fadd2_rn(V1, wu);
+                                V2 = __ffma2_rn(make_float2(omr2, omr2), u, V2);
                                 Ms += omr;
-                                Txx += wux * ux;
-                                Txy += wux * uy;
-                                Tyy += wuy * uy;
+                                Tdiag = __ffma2_rn(wu, u, Tdiag);
+                                Txy += wu.x * u.y;
+                                // sum w (x_j - x_prev_j); the velocities follow at the end
                                 const float2 qp = __ldg(prev + ra[r] + t);
-                                Dx += omr * ((q.x - qp.x) * inv_dt - vix);
-                                Dy += omr * ((q.y - qp.y) * inv_dt - viy);
+                                Dsum = __ffma2_rn(w2, __fadd2_rn(q, make_float2(-qp.x, -qp.y)), Dsum);
                             }
                         }
                     }
@@ -180,6 +179,10 @@ k_features(Ctx c, const float2 *__restrict__ pos, const float2 *__restrict__ pre
     mask01[i] = make_ulonglong2(m[0], m[1]);
     mask2[i] = m[2];
     nbcount[i] = degenerate ? (unsigned short)65535 : (unsigned short)(count < 65534 ? count : 65534);
+    const float V1x = V1.x, V1y = V1.y, V2x = V2.x, V2y = V2.y;
+    const float Txx = Tdiag.x, Tyy = Tdiag.y;
+    // sum w (v_j - v_i) = (sum w (x_j - x_prev_j)) / dt - v_i sum w
+    const float Dx = Dsum.x * inv_dt - vix * Ms, Dy = Dsum.y * inv_dt - viy * Ms;
 
     const float k = __ldg(&S->P.k), kn = __ldg(&S->P.k_near), ks = __ldg(&S->P.k_spring);
     const float rest = __ldg(&S->P.rest_density);
