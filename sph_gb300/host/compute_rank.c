@@ -6,9 +6,10 @@
  * tunables, a 15 x 15/aspect box, h = 2 x the initial particle spacing, a
  * 100-particle bucket cap and 400-entry lists), the particles live in the
  * caller's AoS array behind a pointer array as in fluid.c:183-197, and each
- * step is one sph_cuda_step.  Every steps_per_frame-th step the stand-in
- * render rank receives the packed short coordinates (fluid.c:356-364) and
- * sends back tunables for the following steps (fluid.c:293-294): it moves
+ * step is one sph_cuda_step.  Every steps_per_frame-th step the packed
+ * short coordinates (fluid.c:356-364) go to the stand-in render rank on a
+ * copy stream, and the stand-in answers the previous frame with tunables
+ * for the following steps (fluid.c:293-294): it moves
  * the mover along the render rank's inactive-mode path (renderer.c:493-532)
  * and cycles the fluid presets x, y, a, b (controls.c:344-401) every
  * `preset_frames` frames.
@@ -169,9 +170,18 @@ int main(int argc, char **argv)
     sph_cuda_t *sim = NULL;
     if (sph_cuda_create(&sim, &params, &box, &grid, n) != SPH_OK) return fail("create");
     if (sph_cuda_upload(sim, ptrs, n) != SPH_OK) return fail("upload");
-    short *coords = NULL;
-    if (sph_cuda_host_alloc((void **)&coords, 2 * (size_t)n * sizeof(short)) != SPH_OK)
-        return fail("host_alloc");
+    /* two page-locked frames: frame f is copied while the steps of frame
+     * f + 1 run, as the reference overlaps its MPI_Isend of the coordinates
+     * with the next steps and waits for it before packing again
+     * (fluid.c:282-287, 356-364); the render stand-in answers each frame
+     * with the tunables of the steps after the next frame boundary, one
+     * frame behind, as the render rank's MPI_Scatterv does
+     * (fluid.c:293-294) */
+    short *coords[2] = {NULL, NULL};
+    for (int b = 0; b < 2; ++b)
+        if (sph_cuda_host_alloc((void **)&coords[b], 2 * (size_t)n * sizeof(short)) != SPH_OK)
+            return fail("host_alloc");
+    int frame = 0, pending = -1;
 
     int sub_step = 0;
     for (int t = 0; t < steps; ++t) {
@@ -179,13 +189,25 @@ int main(int argc, char **argv)
         fwrite(tp, sizeof(*tp), 1, ftp);
         if (sph_cuda_step(sim, tp, 1) != SPH_OK) return fail("step");
         if (sub_step == steps_per_frame - 1) {
-            if (sph_cuda_pack_coords_short(sim, coords, n) != SPH_OK) return fail("pack");
-            if (render_frame(&r, coords, n, box.max_x, box.max_y, tp)) {
-                fprintf(stderr, "compute_rank: render stand-in failed\n");
-                return 1;
+            if (pending >= 0) {  /* the previous frame: arrived while this one ran */
+                if (sph_cuda_coords_wait(sim, coords[pending]) != SPH_OK) return fail("wait");
+                if (render_frame(&r, coords[pending], n, box.max_x, box.max_y, tp)) {
+                    fprintf(stderr, "compute_rank: render stand-in failed\n");
+                    return 1;
+                }
             }
+            pending = frame & 1;
+            if (sph_cuda_pack_coords_async(sim, coords[pending], n) != SPH_OK) return fail("pack");
+            ++frame;
         }
         sub_step = sub_step == steps_per_frame - 1 ? 0 : sub_step + 1;
+    }
+    if (pending >= 0) {
+        if (sph_cuda_coords_wait(sim, coords[pending]) != SPH_OK) return fail("wait");
+        if (render_frame(&r, coords[pending], n, box.max_x, box.max_y, tp)) {
+            fprintf(stderr, "compute_rank: render stand-in failed\n");
+            return 1;
+        }
     }
     if (sph_cuda_download(sim, ptrs, n) != SPH_OK) return fail("download");
     double diag[3];
@@ -202,7 +224,8 @@ int main(int argc, char **argv)
     printf("particles %d steps %llu frames %d mean_density %.6f kinetic_energy %.6f "
            "max_cell_occupancy %u\n",
            n, (unsigned long long)cnt.steps, r.nframes, diag[0], diag[2], cnt.max_cell_occupancy);
-    sph_cuda_host_free(coords);
+    sph_cuda_host_free(coords[0]);
+    sph_cuda_host_free(coords[1]);
     sph_cuda_destroy(sim);
     free(ptrs);
     free(particles);
