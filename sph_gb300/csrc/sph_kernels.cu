@@ -27,6 +27,22 @@
 #include "sph_device.cuh"
 #include "sph_learned.h"
 
+// Unroll factors of the candidate filter loops and the relaxation's
+// register budget (tuned on GB300).
+#ifndef SPH_VISC_UNROLL
+#define SPH_VISC_UNROLL 4
+#endif
+#ifndef SPH_DENS_UNROLL
+#define SPH_DENS_UNROLL 2
+#endif
+#ifndef SPH_RELAX_MIN_BLOCKS
+#define SPH_RELAX_MIN_BLOCKS 4  // resident 256-thread CTAs per SM the relaxation is built for
+#endif
+namespace sph {
+constexpr int kViscUnroll = SPH_VISC_UNROLL;
+constexpr int kDensUnroll = SPH_DENS_UNROLL;
+}  // namespace sph
+
 namespace sph {
 
 // ---------------------------------------------------------------------------
@@ -348,7 +364,7 @@ __device__ __forceinline__ void viscosity_predict_one(
                     // 32-bit halves: cheaper bit operations than one 64-bit mask
                     unsigned lo = 0u, hi = 0u;
                     const int n0 = min(len, 32);
-#pragma unroll 4
+#pragma unroll kViscUnroll
                     for (int t = 0; t < n0; ++t) {
                         float2 e;
                         const float r2 = dist2_packed(mp, __ldg(row + t), e);
@@ -356,7 +372,7 @@ __device__ __forceinline__ void viscosity_predict_one(
                         // impulse skips them (r2 == 0)
                         lo |= (unsigned)(r2 <= h2) << t;
                     }
-#pragma unroll 4
+#pragma unroll kViscUnroll
                     for (int t = 32; t < len; ++t) {
                         float2 e;
                         const float r2 = dist2_packed(mp, __ldg(row + t), e);
@@ -451,7 +467,7 @@ __device__ __forceinline__ void density_one(int i, const Ctx &c, const float2 *_
 #pragma unroll
                 for (int hh = 0; hh < 2; ++hh) {
                     const int t1 = hh == 0 ? min(len, 32) : min(len, kMaskRow);
-#pragma unroll 4
+#pragma unroll kDensUnroll
                     for (int t = 32 * hh; t < t1; ++t) {
                         float2 e;
                         const float r2 = dist2_packed(mp, __ldg(row + t), e);
@@ -722,7 +738,7 @@ __device__ __forceinline__ void relax_update_one(
 }
 
 template <bool PROBE, bool PERSIST = false>
-__global__ void __launch_bounds__(kBlock, 4)
+__global__ void __launch_bounds__(kBlock, SPH_RELAX_MIN_BLOCKS)
 k_relax_update(Ctx c, const float4 *__restrict__ xr, const ulonglong2 *__restrict__ mask01,
                const unsigned long long *__restrict__ mask2, const float2 *__restrict__ prev,
                const int *__restrict__ ids, const int *__restrict__ start,
