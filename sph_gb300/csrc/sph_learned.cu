@@ -4,13 +4,14 @@
 //                feature rows and neighbour counts (replaces k_density in a
 //                learned step; writes the same density records and masks)
 //   k_mlp        fused 2-layer width-128 GELU MLP on the tcgen05 tensor cores:
-//                persistent CTAs of 128 threads, weights resident in shared
-//                memory, FP32 accumulators in tensor memory
-//   (k_relax_update then applies the network's displacement, or the plain
-//    relaxation where the predicted density error is too large)
+//                one CTA per SM of four 256-thread pipelines, weights
+//                resident in shared memory, FP32 accumulators in tensor memory
+//   (k_relax_learned then applies the network's displacement and lists the
+//    particles that take the plain relaxation for k_relax_fallback)
 //
 // Training: a generic tcgen05 GEMM (strided BF16 operands staged in shared
-// memory, FP32 accumulation), bias/GELU kernels, Adam on FP32 master weights.
+// memory, FP32 accumulation), bias/activation kernels, Adam on FP32 master
+// weights; sample collection and the calibration of the error output.
 #include <algorithm>
 #include <cstddef>
 #include <cmath>
@@ -656,12 +657,6 @@ __global__ void k_f32_to_bf16(int n, const float *__restrict__ in, __nv_bfloat16
     if (e < n) out[e] = __float2bfloat16(in[e]);
 }
 
-__global__ void k_bf16_to_f32(int n, const __nv_bfloat16 *__restrict__ in, float *__restrict__ out)
-{
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e < n) out[e] = __bfloat162float(in[e]);
-}
-
 // ---------------------------------------------------------------------------
 // sample collection and calibration
 // ---------------------------------------------------------------------------
@@ -761,7 +756,6 @@ __global__ void k_wait_selftest(unsigned *__restrict__ gave_up)
 
 // The learned-relaxation model.
 struct LearnedModel {
-    std::vector<float> host_w;  // FP32 master copy on the host (for get/set)
     float *w = nullptr;         // FP32 master weights (device)
     float *g = nullptr, *m = nullptr, *v = nullptr;
     __nv_bfloat16 *wbf = nullptr;
@@ -979,9 +973,6 @@ int train_loop(LearnedModel *l, int first, int nsamples, int epochs, int batch, 
     }
     LTRY(check_err(l));
     if (loss) *loss = (float)last;
-    std::vector<float> w(NPARAM);
-    LCUDA(cudaMemcpy(w.data(), l->w, NPARAM * sizeof(float), cudaMemcpyDeviceToHost));
-    l->host_w = w;
     return SPH_OK;
 }
 
@@ -1138,7 +1129,6 @@ int sph_learned_create(sph_learned_t **out, int max_samples, unsigned long long 
     fill(ml::OFF_W1, ml::HID, ml::IN);
     fill(ml::OFF_W2, ml::HID, ml::HID);
     fill(ml::OFF_W3, ml::OUT, ml::HID);
-    l->host_w = w;
     rc = sph_learned_set_params(l, w.data());
     if (rc) return fail(rc);
     *out = l;
@@ -1180,7 +1170,6 @@ int sph_learned_set_params(sph_learned_t *l, const float *in)
     ml::k_f32_to_bf16<<<nblk(ml::NPARAM), 256, 0, l->stream>>>(ml::NPARAM, l->w, l->wbf);
     LCUDA(cudaStreamSynchronize(l->stream));
     l->adam_t = 0;
-    l->host_w.assign(in, in + ml::NPARAM);
     return SPH_OK;
 }
 
