@@ -211,6 +211,18 @@ int sph_cuda_pack_coords_short(sph_cuda_t *h, short *coords, int n);
 int sph_cuda_pack_coords_async(sph_cuda_t *h, short *coords, int n);
 int sph_cuda_coords_wait(sph_cuda_t *h, const short *coords);
 
+/* ---- checkpoint / resume ---- */
+
+/* Writes the handle's particles (the reference's fluid_particle records, by
+ * id), its step count and whether the neighbour relation of the current
+ * positions exists to a binary file (48-byte header "SPHCKPT1", then the
+ * records).  sph_cuda_load_state restores such a file into a handle with the
+ * same scenes: the steps that follow are bit-identical to those the saved
+ * handle would have taken.  Also the format of the learned relaxation's
+ * training trajectories. */
+int sph_cuda_save_state(sph_cuda_t *h, const char *path);
+int sph_cuda_load_state(sph_cuda_t *h, const char *path);
+
 /* Rebuilds the neighbour relation on the current positions, like
  * hash_fluid(.., false) (fluid.c:341): after it, the next step applies
  * viscosity impulses even if it is the first step after an upload. */
@@ -319,6 +331,23 @@ int sph_render_liquid(const short *coords, int n, int width, int height, unsigne
                       unsigned char *alpha);
 int sph_cuda_render_liquid(sph_cuda_t *h, int width, int height, unsigned char *rgb,
                            unsigned char *alpha);
+
+/* Bounds-checked builds (compiled with -DSPH_BOUNDS_CHECK, a stand-in for a
+ * memory checker): every data-dependent index of the step's kernels -- a
+ * neighbour slot, a cell key, a scatter or permute destination, a cell
+ * start -- is tested before its access, and a bad one is skipped and
+ * recorded.  sph_cuda_bounds_errors returns the recorded kinds (bit 0
+ * neighbour slot, 1 cell key, 2 scatter/permute destination, 3 cell start;
+ * always 0 in normal builds), sph_cuda_bounds_checked whether this library
+ * is such a build. */
+int sph_cuda_bounds_errors(unsigned *flags);
+int sph_cuda_bounds_checked(void);
+
+/* Test hook for failure handling: after `after` more successful device or
+ * pinned-host allocations of the library (handle creation, scratch and
+ * staging buffers), the next one fails as if memory were exhausted (no
+ * device fault involved); -1 turns it off.  Process-wide. */
+int sph_cuda_debug_fail_allocation(int after);
 
 /* ---- live tunables (host helpers, no device work) ---- */
 

@@ -12,7 +12,9 @@ import re
 import numpy as np
 
 PKG = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(PKG, "lib", "libsph_cuda.so")
+# SPH_CUDA_LIB selects another build of the library (e.g. the bounds-checked
+# lib/libsph_cuda_checked.so) for this process.
+LIB_PATH = os.environ.get("SPH_CUDA_LIB") or os.path.join(PKG, "lib", "libsph_cuda.so")
 INCLUDE = os.path.join(os.path.dirname(PKG), "include")
 
 c_float_p = ctypes.POINTER(ctypes.c_float)
@@ -139,6 +141,8 @@ _SIGS = {
     "sph_cuda_pack_coords_async": (ctypes.c_int, [_P, c_short_p, ctypes.c_int]),
     "sph_cuda_coords_wait": (ctypes.c_int, [_P, c_short_p]),
     "sph_cuda_rebuild_neighbors": (ctypes.c_int, [_P]),
+    "sph_cuda_save_state": (ctypes.c_int, [_P, ctypes.c_char_p]),
+    "sph_cuda_load_state": (ctypes.c_int, [_P, ctypes.c_char_p]),
     "sph_cuda_synchronize": (ctypes.c_int, [_P]),
     "sph_cuda_get_counters": (ctypes.c_int, [_P, ctypes.POINTER(Counters)]),
     "sph_cuda_diagnostics": (ctypes.c_int, [_P, c_double_p]),
@@ -156,6 +160,9 @@ _SIGS = {
     "sph_cuda_timer_stop": (ctypes.c_int, [_P, c_float_p]),
     "sph_cuda_host_alloc": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_size_t]),
     "sph_cuda_host_free": (ctypes.c_int, [_P]),
+    "sph_cuda_debug_fail_allocation": (ctypes.c_int, [ctypes.c_int]),
+    "sph_cuda_bounds_errors": (ctypes.c_int, [ctypes.POINTER(ctypes.c_uint)]),
+    "sph_cuda_bounds_checked": (ctypes.c_int, []),
     "sph_cuda_last_error": (ctypes.c_char_p, []),
     "sph_cuda_abi_sizes": (ctypes.c_int, [c_int_p, ctypes.c_int]),
     # learned relaxation (include/sph_learned.h)

@@ -20,6 +20,7 @@ INCLUDE = os.path.join(ROOT, "include")
 OBJ = os.path.join(ROOT, "_build")
 LIB_DIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIB_DIR, "libsph_cuda.so")
+CHECKED_LIB = os.path.join(LIB_DIR, "libsph_cuda_checked.so")
 HOST = os.path.join(PKG, "host")
 COMPUTE_RANK = os.path.join(LIB_DIR, "sph_compute_rank")
 
@@ -42,11 +43,15 @@ def sources() -> list:
 def _stale() -> bool:
     if not os.path.exists(LIB):
         return True
-    t = os.path.getmtime(LIB)
+    return not os.path.exists(COMPUTE_RANK) or _stale_against(LIB)
+
+
+def _stale_against(lib: str) -> bool:
+    t = os.path.getmtime(lib)
     deps = sources() + glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(CSRC, "*.cuh")) \
         + glob.glob(os.path.join(INCLUDE, "*.h")) + glob.glob(os.path.join(HOST, "*.c")) \
         + [os.path.abspath(__file__)]
-    return not os.path.exists(COMPUTE_RANK) or any(os.path.getmtime(d) > t for d in deps)
+    return any(os.path.getmtime(d) > t for d in deps)
 
 
 def build_host(verbose: bool = False) -> str:
@@ -63,18 +68,15 @@ def build_host(verbose: bool = False) -> str:
     return COMPUTE_RANK
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
-    """Compiles libsph_cuda.so if needed; returns its path."""
-    if not force and not _stale():
-        return LIB
-    os.makedirs(OBJ, exist_ok=True)
+def _compile_lib(lib: str, obj_dir: str, extra: list, verbose: bool) -> None:
+    os.makedirs(obj_dir, exist_ok=True)
     os.makedirs(LIB_DIR, exist_ok=True)
     procs = []
     objs = []
     for src in sources():
-        obj = os.path.join(OBJ, os.path.basename(src)[:-3] + ".o")
+        obj = os.path.join(obj_dir, os.path.basename(src)[:-3] + ".o")
         objs.append(obj)
-        cmd = [nvcc()] + NVCC_FLAGS + ["-c", src, "-o", obj]
+        cmd = [nvcc()] + NVCC_FLAGS + extra + ["-c", src, "-o", obj]
         if verbose:
             print(" ".join(cmd), file=sys.stderr)
         procs.append((src, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
@@ -88,16 +90,34 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if failed:
         msg = "\n".join(f"--- {s}\n{o}" for s, o in failed)
         raise RuntimeError(f"nvcc failed:\n{msg}")
-    tmp = LIB + ".tmp"
+    tmp = lib + ".tmp"
     cmd = [nvcc()] + ARCH + ["-shared", "-cudart", "static", "-o", tmp] + objs
     if verbose:
         print(" ".join(cmd), file=sys.stderr)
     r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
     if r.returncode != 0:
         raise RuntimeError("nvcc link failed:\n" + r.stdout.decode(errors="replace"))
-    os.replace(tmp, LIB)
+    os.replace(tmp, lib)
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    """Compiles libsph_cuda.so (and the compute-rank program) if needed;
+    returns the library's path."""
+    if not force and not _stale():
+        return LIB
+    _compile_lib(LIB, OBJ, [], verbose)
     build_host(verbose)
     return LIB
+
+
+def build_checked(force: bool = False, verbose: bool = False) -> str:
+    """The bounds-checked variant (-DSPH_BOUNDS_CHECK), libsph_cuda_checked.so:
+    every data-dependent index of the step's kernels is tested before its
+    access and a bad one is recorded (sph_cuda_bounds_errors)."""
+    if not force and os.path.exists(CHECKED_LIB) and not _stale_against(CHECKED_LIB):
+        return CHECKED_LIB
+    _compile_lib(CHECKED_LIB, os.path.join(OBJ, "checked"), ["-DSPH_BOUNDS_CHECK"], verbose)
+    return CHECKED_LIB
 
 
 if __name__ == "__main__":

@@ -1,6 +1,8 @@
 // sph_capi.cu -- handle lifecycle and the device-resident C API of libsph_cuda.
 #include <algorithm>
+#include <atomic>
 #include <cstdarg>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cmath>
@@ -46,12 +48,47 @@ int cuda_fail(cudaError_t e, const char *what)
     } while (0)
 #define SPH_CUDA(call) SPH_TRY(cuda_fail((call), #call))
 
+// Test hook (sph_cuda_debug_fail_allocation): the allocation after `after`
+// more successful ones reports cudaErrorMemoryAllocation without
+// allocating; -1 = off.  Process-wide, host-side only.
+static std::atomic<int> g_alloc_fail_after{-1};
+
+static cudaError_t device_alloc(void **p, size_t bytes)
+{
+    int k = g_alloc_fail_after.load();
+    while (k >= 0) {
+        if (g_alloc_fail_after.compare_exchange_weak(k, k - 1)) {
+            if (k == 0) {
+                *p = nullptr;
+                return cudaErrorMemoryAllocation;
+            }
+            break;
+        }
+    }
+    return cudaMalloc(p, bytes);
+}
+
+static cudaError_t host_alloc(void **p, size_t bytes)
+{
+    int k = g_alloc_fail_after.load();
+    while (k >= 0) {
+        if (g_alloc_fail_after.compare_exchange_weak(k, k - 1)) {
+            if (k == 0) {
+                *p = nullptr;
+                return cudaErrorMemoryAllocation;
+            }
+            break;
+        }
+    }
+    return cudaHostAlloc(p, bytes, cudaHostAllocDefault);
+}
+
 template <class T>
 static int dalloc(T **p, size_t count)
 {
     *p = nullptr;
     if (count == 0) count = 1;
-    return cuda_fail(cudaMalloc((void **)p, count * sizeof(T)), "cudaMalloc");
+    return cuda_fail(device_alloc((void **)p, count * sizeof(T)), "cudaMalloc");
 }
 
 int ensure_scratch(sph_cuda *h, size_t bytes)
@@ -60,7 +97,7 @@ int ensure_scratch(sph_cuda *h, size_t bytes)
     if (h->d_scratch) cudaFree(h->d_scratch);
     h->d_scratch = nullptr;
     h->d_scratch_bytes = 0;
-    SPH_CUDA(cudaMalloc(&h->d_scratch, bytes));
+    SPH_CUDA(device_alloc(&h->d_scratch, bytes));
     h->d_scratch_bytes = bytes;
     return SPH_OK;
 }
@@ -71,7 +108,7 @@ int ensure_stage(sph_cuda *h, size_t bytes)
     if (h->h_stage) cudaFreeHost(h->h_stage);
     h->h_stage = nullptr;
     h->h_stage_bytes = 0;
-    SPH_CUDA(cudaHostAlloc(&h->h_stage, bytes, cudaHostAllocDefault));
+    SPH_CUDA(host_alloc(&h->h_stage, bytes));
     h->h_stage_bytes = bytes;
     return SPH_OK;
 }
@@ -310,8 +347,8 @@ static int build_handle(sph_cuda **out, std::vector<Scene> &&scenes, int capacit
         if (rc) return fail(rc);
     }
     h->params_ring = 64;
-    rc = cuda_fail(cudaHostAlloc((void **)&h->h_params_ring,
-                                 h->params_ring * sizeof(tunable_parameters), cudaHostAllocDefault),
+    rc = cuda_fail(host_alloc((void **)&h->h_params_ring,
+                              h->params_ring * sizeof(tunable_parameters)),
                    "cudaHostAlloc");
     if (rc) return fail(rc);
     h->params_ev = new (std::nothrow) cudaEvent_t[h->params_ring]();
@@ -673,11 +710,30 @@ int sph_cuda_pack_coords_async(sph_cuda_t *h, short *coords, int n)
         return SPH_ERR_INVALID;
     }
     if (!h->copy_stream) {
-        SPH_CUDA(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
-        for (int k = 0; k < 2; ++k) {
-            SPH_CUDA(cudaMalloc(&h->d_coords[k], ((size_t)h->capacity + 1) * sizeof(short2)));
-            SPH_CUDA(cudaEventCreateWithFlags(&h->pack_ev[k], cudaEventDisableTiming));
-            SPH_CUDA(cudaEventCreateWithFlags(&h->copy_ev[k], cudaEventDisableTiming));
+        // all or nothing: a failed set-up leaves no half-made resources
+        auto undo = [&]() {
+            for (int k = 0; k < 2; ++k) {
+                if (h->d_coords[k]) cudaFree(h->d_coords[k]);
+                if (h->pack_ev[k]) cudaEventDestroy(h->pack_ev[k]);
+                if (h->copy_ev[k]) cudaEventDestroy(h->copy_ev[k]);
+                h->d_coords[k] = nullptr;
+                h->pack_ev[k] = h->copy_ev[k] = nullptr;
+            }
+        };
+        int rc = SPH_OK;
+        for (int k = 0; k < 2 && !rc; ++k) {
+            rc = cuda_fail(device_alloc((void **)&h->d_coords[k],
+                                        ((size_t)h->capacity + 1) * sizeof(short2)), "cudaMalloc");
+            if (!rc) rc = cuda_fail(cudaEventCreateWithFlags(&h->pack_ev[k], cudaEventDisableTiming),
+                                    "cudaEventCreate");
+            if (!rc) rc = cuda_fail(cudaEventCreateWithFlags(&h->copy_ev[k], cudaEventDisableTiming),
+                                    "cudaEventCreate");
+        }
+        if (!rc) rc = cuda_fail(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking),
+                                "cudaStreamCreate");
+        if (rc) {
+            undo();
+            return rc;
         }
     }
     const int k = h->pack_slot;
@@ -706,6 +762,95 @@ int sph_cuda_coords_wait(sph_cuda_t *h, const short *coords)
         }
     set_error("no pending coordinate copy into %p", (const void *)coords);
     return SPH_ERR_STATE;
+}
+
+// Checkpoint file: header, then n fluid_particle records by id.
+struct CheckpointHeader {
+    char magic[8];           // "SPHCKPT1"
+    uint32_t version;        // 1
+    int32_t n;               // particles (all scenes)
+    int32_t nscenes;
+    uint32_t lists_valid;    // the neighbour relation of the positions exists
+    uint64_t steps;          // steps since the last upload
+    uint32_t record_bytes;   // sizeof(fluid_particle)
+    uint32_t reserved[3];
+};
+static_assert(sizeof(CheckpointHeader) == 48, "checkpoint header layout");
+
+int sph_cuda_save_state(sph_cuda_t *h, const char *path)
+{
+    SPH_TRY(check_handle(h));
+    if (!path) {
+        set_error("null path");
+        return SPH_ERR_INVALID;
+    }
+    const int n = h->n;
+    std::vector<fluid_particle> ps((size_t)n + 1);
+    SPH_TRY(sph_cuda_download_particles(h, ps.data(), n));
+    DevState st;
+    SPH_CUDA(cudaMemcpy(&st, h->d_state, sizeof(st), cudaMemcpyDeviceToHost));
+    CheckpointHeader hd;
+    std::memset(&hd, 0, sizeof(hd));
+    std::memcpy(hd.magic, "SPHCKPT1", 8);
+    hd.version = 1;
+    hd.n = n;
+    hd.nscenes = h->nscenes;
+    hd.lists_valid = st.lists_valid;
+    hd.steps = st.steps;
+    hd.record_bytes = sizeof(fluid_particle);
+    FILE *f = std::fopen(path, "wb");
+    if (!f) {
+        set_error("cannot open %s for writing", path);
+        return SPH_ERR_INVALID;
+    }
+    const bool ok = std::fwrite(&hd, sizeof(hd), 1, f) == 1 &&
+                    (n == 0 || std::fwrite(ps.data(), sizeof(fluid_particle), (size_t)n, f) == (size_t)n);
+    const bool closed = std::fclose(f) == 0;
+    if (!ok || !closed) {
+        set_error("writing %s failed", path);
+        return SPH_ERR_INVALID;
+    }
+    return SPH_OK;
+}
+
+int sph_cuda_load_state(sph_cuda_t *h, const char *path)
+{
+    SPH_TRY(check_handle(h));
+    if (!path) {
+        set_error("null path");
+        return SPH_ERR_INVALID;
+    }
+    FILE *f = std::fopen(path, "rb");
+    if (!f) {
+        set_error("cannot open %s", path);
+        return SPH_ERR_INVALID;
+    }
+    CheckpointHeader hd;
+    std::vector<fluid_particle> ps;
+    bool ok = std::fread(&hd, sizeof(hd), 1, f) == 1 && std::memcmp(hd.magic, "SPHCKPT1", 8) == 0 &&
+              hd.version == 1 && hd.record_bytes == sizeof(fluid_particle) && hd.n >= 0;
+    if (ok && (hd.nscenes != h->nscenes || hd.n > h->capacity)) {
+        std::fclose(f);
+        set_error("checkpoint of %d particles in %d scenes does not fit this handle (%d scenes, "
+                  "capacity %d)", hd.n, hd.nscenes, h->nscenes, h->capacity);
+        return SPH_ERR_INVALID;
+    }
+    if (ok) {
+        ps.resize((size_t)hd.n + 1);
+        ok = hd.n == 0 || std::fread(ps.data(), sizeof(fluid_particle), (size_t)hd.n, f) == (size_t)hd.n;
+    }
+    std::fclose(f);
+    if (!ok) {
+        set_error("%s is not a libsph_cuda checkpoint (or is truncated)", path);
+        return SPH_ERR_INVALID;
+    }
+    SPH_TRY(sph_cuda_upload_particles(h, ps.data(), hd.n));
+    // the upload starts counters afresh: restore the step count and whether
+    // the next step applies viscosity
+    SPH_CUDA(cudaMemcpy(&h->d_state->steps, &hd.steps, sizeof(hd.steps), cudaMemcpyHostToDevice));
+    SPH_CUDA(cudaMemcpy(&h->d_state->lists_valid, &hd.lists_valid, sizeof(hd.lists_valid),
+                        cudaMemcpyHostToDevice));
+    return SPH_OK;
 }
 
 int sph_cuda_rebuild_neighbors(sph_cuda_t *h)
@@ -1031,6 +1176,31 @@ int sph_cuda_host_alloc(void **ptr, size_t bytes)
     }
     *ptr = nullptr;
     SPH_CUDA(cudaHostAlloc(ptr, bytes ? bytes : 1, cudaHostAllocDefault));
+    return SPH_OK;
+}
+
+int sph_cuda_bounds_errors(unsigned *flags)
+{
+    if (!flags) {
+        set_error("null output");
+        return SPH_ERR_INVALID;
+    }
+    *flags = bounds_flags_kernels() | bounds_flags_learned();
+    return SPH_OK;
+}
+
+int sph_cuda_bounds_checked(void)
+{
+#ifdef SPH_BOUNDS_CHECK
+    return 1;
+#else
+    return 0;
+#endif
+}
+
+int sph_cuda_debug_fail_allocation(int after)
+{
+    g_alloc_fail_after.store(after < 0 ? -1 : after);
     return SPH_OK;
 }
 

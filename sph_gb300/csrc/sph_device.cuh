@@ -143,6 +143,38 @@ __device__ __forceinline__ float dist2_packed(float2 mp, float2 q, float2 &d)
     return __fadd_rn(s.x, s.y);
 }
 
+// Checked builds (-DSPH_BOUNDS_CHECK, the stand-in for a memory checker):
+// every index that comes from data -- neighbour slots from cell starts and
+// hit masks, cell keys, scatter and permute destinations -- is tested
+// before its access; a bad one records its kind in a per-translation-unit
+// device flag and the access is skipped (no trap, no fault).  Normal builds
+// compile the tests away.
+enum BoundsKind : unsigned {
+    kBadSlot = 1u,      // neighbour slot outside [0, n)
+    kBadKey = 2u,       // cell key outside [0, M)
+    kBadScatter = 4u,   // scatter / permute destination outside [0, n)
+    kBadStart = 8u      // cell start index outside [0, M]
+};
+#ifdef SPH_BOUNDS_CHECK
+static __device__ unsigned g_bounds_flag;
+__device__ __forceinline__ bool in_bounds(long long i, long long n, unsigned kind)
+{
+    if (i >= 0 && i < n) return true;
+    atomicOr(&g_bounds_flag, kind);
+    return false;
+}
+// Host side, per translation unit: the flags recorded by its kernels.
+static inline unsigned read_bounds_flag()
+{
+    unsigned v = 0;
+    cudaMemcpyFromSymbol(&v, g_bounds_flag, sizeof(v));
+    return v;
+}
+#else
+__device__ __forceinline__ bool in_bounds(long long, long long, unsigned) { return true; }
+static inline unsigned read_bounds_flag() { return 0u; }
+#endif
+
 // Visits the candidate slots of the 3x3 cell stencil around `key` in sorted
 // order.  Without bucket overflow, the three cells of a stencil row are
 // contiguous in the sorted arrays, so each row is one range
@@ -152,7 +184,7 @@ __device__ __forceinline__ float dist2_packed(float2 mp, float2 q, float2 &d)
 template <class F>
 __device__ __forceinline__ void for_each_candidate(unsigned key, const int *__restrict__ start,
                                                    const SG &g, bool capped, int max_bucket,
-                                                   F &&f)
+                                                   int n, F &&f)
 {
     const int lk = (int)key - g.c_off;
     const int gy = lk / g.size_x;
@@ -165,13 +197,15 @@ __device__ __forceinline__ void for_each_candidate(unsigned key, const int *__re
         const int row = g.c_off + y * g.size_x;
         if (!capped) {
             const int a = __ldg(start + row + x0), b = __ldg(start + row + x1 + 1);
-            for (int j = a; j < b; ++j) f(j);
+            for (int j = a; j < b; ++j)
+                if (in_bounds(j, n, kBadSlot)) f(j);
         } else {
             for (int x = x0; x <= x1; ++x) {
                 const int a = __ldg(start + row + x);
                 const int e = __ldg(start + row + x + 1);
                 const int b = e - a > max_bucket ? a + max_bucket : e;
-                for (int j = a; j < b; ++j) f(j);
+                for (int j = a; j < b; ++j)
+                    if (in_bounds(j, n, kBadSlot)) f(j);
             }
         }
     }
@@ -191,7 +225,7 @@ __device__ __forceinline__ bool searchable(unsigned key, int slot, const int *__
 // contiguous range [a[r], a[r] + len[r]) of sorted slots (empty outside the
 // grid).  Valid when no cell overflowed its bucket cap.
 __device__ __forceinline__ void stencil_rows(unsigned key, const int *__restrict__ start,
-                                             const SG &g, int (&a)[3], int (&len)[3])
+                                             const SG &g, int (&a)[3], int (&len)[3], int n)
 {
     const int lk = (int)key - g.c_off;
     const int gy = lk / g.size_x;
@@ -208,6 +242,9 @@ __device__ __forceinline__ void stencil_rows(unsigned key, const int *__restrict
             const int row = g.c_off + y * g.size_x;
             a[r] = __ldg(start + row + x0);
             len[r] = __ldg(start + row + x1 + 1) - a[r];
+            // checked builds: a row outside [0, n) is reported and emptied
+            if (len[r] > 0 && !(in_bounds(a[r], n, kBadStart) && in_bounds(a[r] + len[r] - 1, n, kBadSlot)))
+                len[r] = 0;
         }
     }
 }
@@ -220,7 +257,8 @@ constexpr int kMaskRow = 64;  // candidates per stencil row recorded in a hit ma
 // particle's neighbours overlap its arithmetic.  The visiting order is the
 // bits' order.
 template <class T, class Load, class Visit>
-__device__ __forceinline__ void walk_mask(unsigned long long m, int base, Load load, Visit visit)
+__device__ __forceinline__ void walk_mask(unsigned long long m, int base, int n, Load load,
+                                          Visit visit)
 {
     unsigned half[2] = {(unsigned)m, (unsigned)(m >> 32)};
     bool have = false;
@@ -232,6 +270,7 @@ __device__ __forceinline__ void walk_mask(unsigned long long m, int base, Load l
         while (b) {
             const int j = base + 32 * hh + __ffs(b) - 1;
             b &= b - 1u;
+            if (!in_bounds(j, n, kBadSlot)) continue;
             const T d = load(j);
             if (have) visit(jp, dp);
             jp = j;

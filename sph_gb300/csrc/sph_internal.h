@@ -40,6 +40,7 @@ struct Ctx {
     int nscenes;
     int n;             // particles of all scenes
     int max_bucket;    // bucket cap, the same in every scene
+    int M;             // cell counters of all scenes (cells + no-cell buckets)
 };
 
 // Device-resident counters and flags of one handle.
@@ -173,6 +174,7 @@ inline Ctx make_ctx(const sph_cuda *h)
     c.nscenes = h->nscenes;
     c.n = h->n;
     c.max_bucket = h->max_bucket;
+    c.M = h->M;
     return c;
 }
 
@@ -182,6 +184,8 @@ int ensure_stage(sph_cuda *h, size_t bytes);
 int upload_soa_device(sph_cuda *h, int n);  // pos_b/vel_b (id order) + xr_c -> state
 int set_scene_params(sph_cuda *h, int scene, const tunable_parameters *tp);
 int enqueue_step(sph_cuda *h, cudaEvent_t *events, int *nkernels);
+unsigned bounds_flags_kernels();  // checked builds (SPH_BOUNDS_CHECK): recorded index faults
+unsigned bounds_flags_learned();
 int enqueue_predicted_state(sph_cuda *h);       // first half of a step: C order + density
 int launch_learned_passes(sph_cuda *h, cudaEvent_t *events);  // features + network (C order)
 int launch_learned_relax(sph_cuda *h, float2 *probe_out, cudaEvent_t *events = nullptr);

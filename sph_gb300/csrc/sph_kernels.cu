@@ -237,7 +237,8 @@ k_scatter_ids(int n, const uint2 *__restrict__ kr, const int *__restrict__ id_sr
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint2 k = kr[i];
-    tmp[__ldg(start + k.x) + (int)k.y] = id_src ? id_src[i] : i;
+    const int d = __ldg(start + k.x) + (int)k.y;
+    if (in_bounds(d, n, kBadScatter)) tmp[d] = id_src ? id_src[i] : i;
 }
 
 // Final position = cell start + number of cell members with a smaller id, so
@@ -264,11 +265,13 @@ k_permute(int n, const uint2 *__restrict__ kr, const int *__restrict__ start,
     int r;
     if (s1 - s0 <= kRankScanMax) {
         r = 0;
-        for (int j = s0; j < s1; ++j) r += __ldg(tmp + j) < myid;
+        for (int j = s0; j < s1; ++j)
+            if (in_bounds(j, n, kBadScatter)) r += __ldg(tmp + j) < myid;
     } else {
         r = (int)k.y;  // pathological cell: arrival order
     }
     const int d = s0 + r;
+    if (!in_bounds(d, n, kBadScatter)) return;
     id_dst[d] = myid;
     a_dst[d] = a_src[i];
     if (b_src) b_dst[d] = b_src[i];
@@ -285,7 +288,7 @@ k_keys(Ctx c, const float2 *__restrict__ pos, uint2 *__restrict__ kr, unsigned *
     const SG g = load_grid(c.scenes + scene_of(c, i));
     const float2 p = pos[i];
     const unsigned key = cell_key(p.x, p.y, g);
-    kr[i] = make_uint2(key, atomicAdd(cnt + key, 1u));
+    kr[i] = make_uint2(key, in_bounds(key, c.M, kBadKey) ? atomicAdd(cnt + key, 1u) : 0u);
 }
 
 // ---------------------------------------------------------------------------
@@ -354,7 +357,7 @@ __device__ __forceinline__ void viscosity_predict_one(
             // two phases: a cheap scan marks the neighbours of each stencil
             // row, then only they pay for the impulse (less SIMT waste)
             int ra[3], rl[3];
-            stencil_rows(key, start, g, ra, rl);
+            stencil_rows(key, start, g, ra, rl, c.n);
             if (rl[0] <= kMaskRow && rl[1] <= kMaskRow && rl[2] <= kMaskRow) {
                 unsigned long long m[3];
 #pragma unroll
@@ -383,12 +386,12 @@ __device__ __forceinline__ void viscosity_predict_one(
                 m[1] &= ~(1ull << (i - ra[1]));  // self
 #pragma unroll
                 for (int r = 0; r < 3; ++r)
-                    walk_mask<float4>(m[r], ra[r], load_pv,
+                    walk_mask<float4>(m[r], ra[r], c.n, load_pv,
                                       [&](int, const float4 &d) { impulse_with(d); });
                 walked = true;
             }
         }
-        if (!walked) for_each_candidate(key, start, g, capped, c.max_bucket, impulse);
+        if (!walked) for_each_candidate(key, start, g, capped, c.max_bucket, c.n, impulse);
     }
     if (PROBE) {
         probe_out[i] = dv;
@@ -400,7 +403,7 @@ __device__ __forceinline__ void viscosity_predict_one(
     float ny = __fadd_rn(p.y, __fmul_rn(v.y, dt));
     boundary_of(nx, ny, S);
     const unsigned k2 = cell_key(nx, ny, g);
-    const unsigned rank = atomicAdd(cnt + k2, 1u);
+    const unsigned rank = in_bounds(k2, c.M, kBadKey) ? atomicAdd(cnt + k2, 1u) : 0u;
     pos_out[i] = make_float2(nx, ny);
     prev_out[i] = p;
     kr_out[i] = make_uint2(k2, rank);
@@ -458,7 +461,7 @@ __device__ __forceinline__ void density_one(int i, const Ctx &c, const float2 *_
     if (searchable(key, i, start, g, capped, c.max_bucket)) {
         if (!capped) {
             int ra[3], rl[3];
-            stencil_rows(key, start, g, ra, rl);
+            stencil_rows(key, start, g, ra, rl, c.n);
 #pragma unroll
             for (int r = 0; r < 3; ++r) {
                 const float2 *row = pos + ra[r];
@@ -508,7 +511,7 @@ __device__ __forceinline__ void density_one(int i, const Ctx &c, const float2 *_
             const int self = i - ra[1];
             if (self < kMaskRow) m[1] &= ~(1ull << self);
         } else {
-            for_each_candidate(key, start, g, true, c.max_bucket, [&](int j) {
+            for_each_candidate(key, start, g, true, c.max_bucket, c.n, [&](int j) {
                 if (j == i) return;
                 const float2 q = __ldg(pos + j);
                 const float r2 = dist2(p.x - q.x, p.y - q.y);
@@ -695,14 +698,14 @@ __device__ __forceinline__ void relax_update_one(
         bool walked = false;
         if (!capped) {
             int ra[3], rl[3];
-            stencil_rows(key, start, g, ra, rl);
+            stencil_rows(key, start, g, ra, rl, cx.n);
             if (rl[0] <= kMaskRow && rl[1] <= kMaskRow && rl[2] <= kMaskRow) {
                 const ulonglong2 m01 = mask01[i];
                 const unsigned long long mm[3] = {m01.x, m01.y, mask2[i]};
 #pragma unroll
                 for (int r = 0; r < 3; ++r)
                     walk_mask<float4>(
-                        mm[r], ra[r], [&](int j) { return __ldg(xr + j); },
+                        mm[r], ra[r], cx.n, [&](int j) { return __ldg(xr + j); },
                         [&](int j, const float4 &q) {
                             relax_pair_walk(wc, p, q, i, j, S, ids, acc, nudges);
                         });
@@ -710,7 +713,7 @@ __device__ __forceinline__ void relax_update_one(
             }
         }
         if (!walked) {
-            for_each_candidate(key, start, g, capped, cx.max_bucket, [&](int j) {
+            for_each_candidate(key, start, g, capped, cx.max_bucket, cx.n, [&](int j) {
                 if (j == i) return;
                 const float4 q = __ldg(xr + j);
                 if (dist2(p.x - q.x, p.y - q.y) > c.h2) return;
@@ -731,7 +734,7 @@ __device__ __forceinline__ void relax_update_one(
     const float vx = clamp5(__fdiv_rn(__fsub_rn(nx, pv.x), dt_end));
     const float vy = clamp5(__fdiv_rn(__fsub_rn(ny, pv.y), dt_end));
     const unsigned k2 = cell_key(nx, ny, load_grid(S));
-    const unsigned rank = atomicAdd(cnt + k2, 1u);
+    const unsigned rank = in_bounds(k2, cx.M, kBadKey) ? atomicAdd(cnt + k2, 1u) : 0u;
     pos_out[i] = make_float2(nx, ny);
     vel_out[i] = make_float2(vx, vy);
     kr_out[i] = make_uint2(k2, rank);
@@ -1192,6 +1195,8 @@ int enqueue_step(sph_cuda *h, cudaEvent_t *events, int *nkernels)
     if (nkernels) *nkernels = e - 1;
     return cuda_fail(cudaGetLastError(), "step launch");
 }
+
+unsigned bounds_flags_kernels() { return read_bounds_flag(); }
 
 const char *kernel_name(int k)
 {

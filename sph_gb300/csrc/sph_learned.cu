@@ -112,7 +112,7 @@ k_features(Ctx c, const float2 *__restrict__ pos, const float2 *__restrict__ pre
     if (searchable(key, i, start, g, capped, c.max_bucket)) {
         if (!capped) {
             int ra[3], rl[3];
-            stencil_rows(key, start, g, ra, rl);
+            stencil_rows(key, start, g, ra, rl, c.n);
 #pragma unroll
             for (int r = 0; r < 3; ++r) {
                 const float2 *row = pos + ra[r];
@@ -160,7 +160,7 @@ k_features(Ctx c, const float2 *__restrict__ pos, const float2 *__restrict__ pre
             if (self < kMaskRow) m[1] &= ~(1ull << self);
         } else {
             degenerate = true;
-            for_each_candidate(key, start, g, true, c.max_bucket, [&](int j) {
+            for_each_candidate(key, start, g, true, c.max_bucket, c.n, [&](int j) {
                 if (j == i) return;
                 const float2 q = __ldg(pos + j);
                 const float r2 = dist2(p.x - q.x, p.y - q.y);
@@ -699,7 +699,7 @@ __global__ void k_density_displaced(Ctx c, const float2 *__restrict__ pos,
     const unsigned key = cell_key(p0.x, p0.y, g);
     float a = 0.0f;
     if (searchable(key, i, start, g, capped, c.max_bucket)) {
-        for_each_candidate(key, start, g, capped, c.max_bucket, [&](int j) {
+        for_each_candidate(key, start, g, capped, c.max_bucket, c.n, [&](int j) {
             if (j == i) return;
             const float2 q = pos[j], dq = disp[j];
             const float r2 = dist2(px - (q.x + dq.x), py - (q.y + dq.y));
@@ -1040,6 +1040,8 @@ int launch_learned_passes(sph_cuda *h, cudaEvent_t *events)
     if (events) cudaEventRecord(events[1], h->stream);
     return SPH_OK;
 }
+
+unsigned bounds_flags_learned() { return read_bounds_flag(); }
 
 void free_learned_buffers(sph_cuda *h)
 {

@@ -205,6 +205,7 @@ extern "C" int sph_cuda_density_static(const float *x, const float *y, int n,
     c.nscenes = 1;
     c.n = n;
     c.max_bucket = sc.max_bucket;
+    c.M = (int)cells + 1;
 
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const int M = sc.ncells + 1;

@@ -160,6 +160,17 @@ class Simulation:
         arr = (_lib.TunableParameters * len(params_list))(*[tunables(p) for p in params_list])
         check(lib().sph_cuda_step_schedule(self._h, arr, len(params_list)))
 
+    def save_state(self, path: str):
+        """Checkpoint (sph_cuda_save_state)."""
+        check(lib().sph_cuda_save_state(self._h, str(path).encode()))
+
+    def load_state(self, path: str):
+        """Resume from a checkpoint (sph_cuda_load_state)."""
+        check(lib().sph_cuda_load_state(self._h, str(path).encode()))
+        import struct
+        with open(path, "rb") as f:
+            self.n = struct.unpack("<i", f.read(16)[12:16])[0]
+
     def rebuild_neighbors(self):
         check(lib().sph_cuda_rebuild_neighbors(self._h))
 
