@@ -561,12 +561,15 @@ def run_gpu(args, world, rank):
     n, cells = work.n, work.cells
     K, W = args.steps, args.warmup
 
-    # ---- launch shapes: tuned on a copy of the scene at step W, so that the
-    # timed steps are steps W .. W+K-1 of the run ----
-    tuner = work.fresh()
-    work.advance(tuner, 0, W)
-    shapes = work.tune(tuner)
-    tuner.close()
+    # ---- launch shapes: given, or tuned on a copy of the scene at step W, so
+    # that the timed steps are steps W .. W+K-1 of the run ----
+    if args.shapes:
+        shapes = [int(v) for v in args.shapes.split(",")]
+    else:
+        tuner = work.fresh()
+        work.advance(tuner, 0, W)
+        shapes = work.tune(tuner)
+        tuner.close()
 
     # ---- device-resident throughput ----
     sim = work.fresh()
@@ -673,6 +676,9 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=262_144)
     ap.add_argument("--cpu-steps", type=int, default=12)
     ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--shapes", default="",
+                    help="six ints: the gathers' launch shapes, instead of autotuning "
+                         "(profiling runs: under a profiler the tuner's timings are not real)")
     ap.add_argument("--no-trajectory", action="store_true")
     ap.add_argument("--learned-threshold", type=float, default=0.01)
     ap.add_argument("--train-scenes", type=int, default=200)
