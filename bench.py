@@ -51,14 +51,12 @@ sys.path.insert(0, ROOT)
 # implementation choice and are not counted as algorithmic.
 ALG_BYTES = {
     "viscosity_predict": (40, 0),   # R pos, vel 16; W pos, prev, key+rank 24
-    "cell_scan_reduce_1": (0, 4),   # R count
-    "cell_scan_apply_1": (0, 12),   # R count, W start, W zero
+    "cell_starts_1": (0, 12),       # R count, W start, W zero
     "cell_scatter_1": (20, 0),      # R key+rank 8, id 4, start 4; W slot 4
     "cell_permute_1": (52, 0),      # R key+rank 8, slots 4, id 4, pos 8, prev 8; W id, pos, prev 20
     "density": (16, 0),             # R pos 8; W rho, rho_near 8
     "relax_update": (40, 0),        # R pos, rho, prev 24; W pos, vel 16
-    "cell_scan_reduce_2": (0, 4),
-    "cell_scan_apply_2": (0, 12),
+    "cell_starts_2": (0, 12),
     "cell_scatter_2": (20, 0),
     "cell_permute_2": (52, 0),      # R key+rank, slots, id, pos, vel; W id, pos, vel
 }

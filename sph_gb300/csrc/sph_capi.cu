@@ -229,7 +229,7 @@ static void free_all(sph_cuda *h)
     if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
     void *ptrs[] = {h->pos_a, h->vel_a, h->id_a, h->pos_b, h->prev_b, h->vel_b, h->kr_b,
                     h->pos_c, h->prev_c, h->xr_c, h->mask01_c, h->mask2_c, h->id_c,
-                    h->tmp_id, h->cnt, h->start_a, h->start_c, h->tile_sums, h->d_scenes,
+                    h->tmp_id, h->cnt, h->start_a, h->start_c, h->tile_sums, h->build_tiles, h->d_scenes,
                     h->d_p_off, h->d_nocell, h->d_state, h->d_partials, h->d_scratch};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -327,6 +327,7 @@ static int build_handle(sph_cuda **out, std::vector<Scene> &&scenes, int capacit
         (rc = dalloc(&h->cnt, std::max(M, N + 1))) ||
         (rc = dalloc(&h->start_a, std::max(M + 1, N + 1))) || (rc = dalloc(&h->start_c, M + 1)) ||
         (rc = dalloc(&h->tile_sums, (size_t)h->ntiles)) ||
+        (rc = dalloc(&h->build_tiles, (size_t)h->ntiles)) ||
         (rc = dalloc(&h->d_scenes, (size_t)h->nscenes)) ||
         (rc = dalloc(&h->d_p_off, (size_t)h->nscenes + 1)) || (rc = dalloc(&h->d_nocell, nwords)) ||
         (rc = dalloc(&h->d_state, 1)) || (rc = dalloc(&h->d_partials, (size_t)h->npartials * 3 + 3)))
@@ -334,6 +335,9 @@ static int build_handle(sph_cuda **out, std::vector<Scene> &&scenes, int capacit
     rc = cuda_fail(cudaMemsetAsync(h->cnt, 0, std::max(M, N + 1) * sizeof(unsigned), h->stream),
                    "cudaMemset");
     if (!rc) rc = cuda_fail(cudaMemsetAsync(h->d_state, 0, sizeof(DevState), h->stream), "cudaMemset");
+    if (!rc)
+        rc = cuda_fail(cudaMemsetAsync(h->build_tiles, 0, (size_t)h->ntiles * sizeof(unsigned), h->stream),
+                       "cudaMemset");
     if (rc) return fail(rc);
     {
         std::vector<unsigned> bits(nwords, 0u);
@@ -887,6 +891,10 @@ int sph_cuda_get_counters(sph_cuda_t *h, sph_cuda_counters *out)
     out->bucket_overflow = s.bucket_overflow;
     out->max_cell_occupancy = s.max_occ;
     out->list_cap_risk = s.list_cap_risk;
+    if (s.tile_count_mismatch) {
+        set_error("internal: a cell build's tile counts disagreed with its cell counters");
+        return SPH_ERR_CUDA;
+    }
     return SPH_OK;
 }
 

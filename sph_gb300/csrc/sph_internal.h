@@ -41,6 +41,9 @@ struct Ctx {
     int n;             // particles of all scenes
     int max_bucket;    // bucket cap, the same in every scene
     int M;             // cell counters of all scenes (cells + no-cell buckets)
+    // particles per scan tile of the build that the kernel's cell keys feed,
+    // counted by the step's key producers (null: not counted)
+    unsigned *tile_cnt = nullptr;
 };
 
 // Device-resident counters and flags of one handle.
@@ -53,7 +56,8 @@ struct DevState {
     unsigned int lists_valid;      // a neighbour relation exists: viscosity is on
     unsigned int build_max_occ[4]; // per build slot, reset by the build's key producer
     unsigned int fb_count;         // learned step: particles on the fallback list
-    unsigned int pad[4];
+    unsigned int tile_count_mismatch;  // a build's tile counts disagreed with its counters
+    unsigned int pad[3];
     unsigned long long learned_steps;     // steps run with a learned model attached
     unsigned long long learned_fallback;  // particle-steps of those that used the plain relaxation
 };
@@ -63,6 +67,11 @@ enum BuildSlot { SLOT_PREDICTED = 0, SLOT_RELAXED = 1, SLOT_UPLOAD = 2, SLOT_PRO
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = 16;                        // per thread
 constexpr int kScanTile = kScanThreads * kScanItems;  // cells per scan tile
+// tiles of a step's cell build (k_cell_starts), counted by the key producers
+constexpr int kBuildThreads = 256;
+constexpr int kBuildItems = 16;
+constexpr int kBuildTile = kBuildThreads * kBuildItems;
+static_assert(kBuildTile >= kScanTile, "the build's tile counts fit the scan tile buffer");
 constexpr int kBlock = 256;                           // default particle-kernel block
 constexpr int kMaxBlock = 512;                        // largest block an autotuner may pick
 constexpr int kRankScanMax = 1024;  // cells above this population use atomic order
@@ -114,6 +123,7 @@ struct sph_cuda {
     int *start_a = nullptr;       // M + 1 cell starts for the *_a order
     int *start_c = nullptr;       // M + 1 cell starts for the *_c order
     int *tile_sums = nullptr;
+    unsigned *build_tiles = nullptr;  // particles per build tile of a step's build (kept zero between builds)
     int ntiles = 0;
 
     sph::DevState *d_state = nullptr;
@@ -175,6 +185,7 @@ inline Ctx make_ctx(const sph_cuda *h)
     c.n = h->n;
     c.max_bucket = h->max_bucket;
     c.M = h->M;
+    c.tile_cnt = h->build_tiles;
     return c;
 }
 

@@ -64,6 +64,19 @@ __device__ __forceinline__ unsigned warp_max(unsigned v)
     return v;
 }
 
+// Counts one particle with cell key `key` into its scan tile: the lanes of
+// the warp that reach this call together and share a tile add with one
+// atomic (the particles of a warp are neighbours in cell order, so most
+// warps issue one or two).
+__device__ __forceinline__ void add_tile_count(unsigned *tile_cnt, unsigned key)
+{
+    if (!tile_cnt) return;
+    const unsigned active = __activemask();
+    const unsigned t = key / (unsigned)kBuildTile;
+    const unsigned peers = __match_any_sync(active, t);
+    if ((threadIdx.x & 31) == (unsigned)(__ffs(peers) - 1)) atomicAdd(tile_cnt + t, (unsigned)__popc(peers));
+}
+
 // Exclusive scan over the block; returns the thread's exclusive prefix and
 // the block total.  `sh` holds one word per warp.
 __device__ __forceinline__ unsigned block_exclusive_scan(unsigned v, unsigned *sh, unsigned &total)
@@ -229,12 +242,152 @@ k_scan_apply(unsigned *__restrict__ in, int M, const int *__restrict__ tile_sums
     if (blockIdx.x == gridDim.x - 1 && threadIdx.x == blockDim.x - 1) out[M] = (int)(prefix + total);
 }
 
+// Cell starts of a step's build in one pass over the counters: the key
+// producers of a step (viscosity_predict, the relaxations) also count their
+// particles per build tile (add_tile_count), so each CTA takes the prefix of
+// the tiles before it from those counts, scans its own tile of counters
+// into starts, zeroes the counters and gathers the occupancy statistics of
+// k_scan_reduce -- with one barrier, so that a CTA's life is one round of
+// loads and one of stores.  It checks its tile's total against the
+// producers' count (DevState::tile_count_mismatch); the build's scatter
+// zeroes the counts afterwards.
+__global__ void __launch_bounds__(kBuildThreads, 1536 / kBuildThreads)
+k_cell_starts(unsigned *__restrict__ in, int M, const unsigned *__restrict__ nocell,
+              const unsigned *__restrict__ tile_cnt, int *__restrict__ out, DevState *st,
+              unsigned *occ, int max_bucket, int max_neighbors)
+{
+    constexpr int ITEMS = kBuildItems, NW = ITEMS >= 32 ? ITEMS / 32 : 1;
+    constexpr int WARPS = kBuildThreads / 32;
+    static_assert(ITEMS % 4 == 0 && (ITEMS == 16 || ITEMS % 32 == 0), "items per thread");
+    __shared__ unsigned sh_sum[WARPS], sh_pre[WARPS], sh_m[WARPS];
+    __shared__ unsigned long long sh_e[WARPS], sh_o[WARPS];
+    const int tile = blockIdx.x;
+    const int base = tile * kBuildTile + threadIdx.x * ITEMS;
+    // prefix of all earlier tiles, from the producers' counts: the loads go
+    // out together with the tile's own counters
+    unsigned acc = 0;
+    {
+        constexpr int kBatch = 4;
+        for (int t0 = 0; t0 < tile; t0 += kBatch * kBuildThreads) {
+            unsigned x[kBatch];
+#pragma unroll
+            for (int j = 0; j < kBatch; ++j) {
+                const int t = t0 + j * kBuildThreads + threadIdx.x;
+                x[j] = t < tile ? __ldcg(tile_cnt + t) : 0u;
+            }
+#pragma unroll
+            for (int j = 0; j < kBatch; ++j) acc += x[j];
+        }
+    }
+    const unsigned expect = threadIdx.x == 0 ? __ldcg(tile_cnt + tile) : 0u;
+    unsigned v[ITEMS];
+    const bool full = base + ITEMS <= M;
+    if (full) {
+        const uint4 *p = reinterpret_cast<const uint4 *>(in + base);
+#pragma unroll
+        for (int q = 0; q < ITEMS / 4; ++q) {
+            const uint4 t = p[q];
+            v[4 * q] = t.x; v[4 * q + 1] = t.y; v[4 * q + 2] = t.z; v[4 * q + 3] = t.w;
+        }
+    } else {
+#pragma unroll
+        for (int e = 0; e < ITEMS; ++e) v[e] = base + e < M ? in[base + e] : 0u;
+    }
+    // the thread's counters in the no-cell bitmap
+    unsigned bits[NW];
+#pragma unroll
+    for (int j = 0; j < NW; ++j)
+        bits[j] = (nocell && base + 32 * j < M) ? __ldg(nocell + (base >> 5) + j) : 0u;
+    if (ITEMS < 32) bits[0] >>= (base & 31);
+    unsigned local = 0, mx = 0;
+    unsigned long long excess = 0, outside = 0;
+#pragma unroll
+    for (int e = 0; e < ITEMS; ++e) {
+        local += v[e];
+        if ((bits[e >> 5] >> (e & 31)) & 1u) {
+            outside += v[e];
+        } else {
+            mx = max(mx, v[e]);
+            if (v[e] > (unsigned)max_bucket) excess += v[e] - max_bucket;
+        }
+    }
+    // warp-level: inclusive scan of the thread sums, reductions of the rest
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned x = local;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    acc = warp_sum(acc);
+    mx = warp_max(mx);
+    excess = warp_sum(excess);
+    outside = warp_sum(outside);
+    if (lane == 31) sh_sum[warp] = x;
+    if (lane == 0) { sh_pre[warp] = acc; sh_m[warp] = mx; sh_e[warp] = excess; sh_o[warp] = outside; }
+    __syncthreads();
+    // every thread combines the per-warp words itself (no second barrier)
+    unsigned before = 0, total = 0, prefix = 0;
+#pragma unroll
+    for (int w = 0; w < WARPS; ++w) {
+        const unsigned sw = sh_sum[w];
+        before += w < warp ? sw : 0u;
+        total += sw;
+        prefix += sh_pre[w];
+    }
+    unsigned run = prefix + before + x - local;
+    if (full) {
+        int4 *o = reinterpret_cast<int4 *>(out + base);
+        uint4 *z = reinterpret_cast<uint4 *>(in + base);
+#pragma unroll
+        for (int q = 0; q < ITEMS / 4; ++q) {
+            int4 t;
+            t.x = (int)run; run += v[4 * q];
+            t.y = (int)run; run += v[4 * q + 1];
+            t.z = (int)run; run += v[4 * q + 2];
+            t.w = (int)run; run += v[4 * q + 3];
+            o[q] = t;
+            z[q] = make_uint4(0, 0, 0, 0);
+        }
+    } else {
+#pragma unroll
+        for (int e = 0; e < ITEMS; ++e) {
+            if (base + e < M) {
+                out[base + e] = (int)run;
+                run += v[e];
+                in[base + e] = 0u;
+            }
+        }
+    }
+    if (tile == (int)gridDim.x - 1 && threadIdx.x == blockDim.x - 1) out[M] = (int)(prefix + total);
+    if (threadIdx.x == 0) {
+        if (total != expect) atomicOr(&st->tile_count_mismatch, 1u);
+        if (occ) {
+            unsigned tm = 0;
+            unsigned long long te = 0, to = 0;
+#pragma unroll
+            for (int w = 0; w < WARPS; ++w) {
+                tm = max(tm, sh_m[w]); te += sh_e[w]; to += sh_o[w];
+            }
+            atomicMax(occ, tm);
+            atomicMax(&st->max_occ, tm);
+            if (te) atomicAdd(&st->bucket_overflow, te);
+            if (to) atomicAdd(&st->out_of_grid, to);
+            const unsigned m = tm < (unsigned)max_bucket ? tm : (unsigned)max_bucket;
+            if (m > 0 && 5u * m - 1u > (unsigned)max_neighbors) atomicOr(&st->list_cap_risk, 1u);
+        }
+    }
+}
+
 // Scratch slot per particle: cell start + arrival rank.
 __global__ void __launch_bounds__(kBlock)
 k_scatter_ids(int n, const uint2 *__restrict__ kr, const int *__restrict__ id_src,
-              const int *__restrict__ start, int *__restrict__ tmp)
+              const int *__restrict__ start, int *__restrict__ tmp, unsigned *tile_cnt, int ntiles)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    // the build's tile counts have been read (k_cell_starts): zero them for
+    // the next build
+    for (int t = i; t < ntiles; t += gridDim.x * blockDim.x) tile_cnt[t] = 0u;
     if (i >= n) return;
     const uint2 k = kr[i];
     const int d = __ldg(start + k.x) + (int)k.y;
@@ -403,7 +556,11 @@ __device__ __forceinline__ void viscosity_predict_one(
     float ny = __fadd_rn(p.y, __fmul_rn(v.y, dt));
     boundary_of(nx, ny, S);
     const unsigned k2 = cell_key(nx, ny, g);
-    const unsigned rank = in_bounds(k2, c.M, kBadKey) ? atomicAdd(cnt + k2, 1u) : 0u;
+    unsigned rank = 0u;
+    if (in_bounds(k2, c.M, kBadKey)) {
+        rank = atomicAdd(cnt + k2, 1u);
+        add_tile_count(c.tile_cnt, k2);
+    }
     pos_out[i] = make_float2(nx, ny);
     prev_out[i] = p;
     kr_out[i] = make_uint2(k2, rank);
@@ -734,7 +891,11 @@ __device__ __forceinline__ void relax_update_one(
     const float vx = clamp5(__fdiv_rn(__fsub_rn(nx, pv.x), dt_end));
     const float vy = clamp5(__fdiv_rn(__fsub_rn(ny, pv.y), dt_end));
     const unsigned k2 = cell_key(nx, ny, load_grid(S));
-    const unsigned rank = in_bounds(k2, cx.M, kBadKey) ? atomicAdd(cnt + k2, 1u) : 0u;
+    unsigned rank = 0u;
+    if (in_bounds(k2, cx.M, kBadKey)) {
+        rank = atomicAdd(cnt + k2, 1u);
+        add_tile_count(cx.tile_cnt, k2);
+    }
     pos_out[i] = make_float2(nx, ny);
     vel_out[i] = make_float2(vx, vy);
     kr_out[i] = make_uint2(k2, rank);
@@ -1045,28 +1206,36 @@ static int launch_scan(sph_cuda *h, unsigned *in, int M, int *out, unsigned *occ
     return SPH_OK;
 }
 
+// The cell starts of a step's build (all M counters, zeroed after) into
+// `out` (M + 1 entries); the build's key producer counted its particles per
+// build tile into build_tiles, which the build's scatter zeroes again.
+static int build_tiles_of(const sph_cuda *h) { return (h->M + kBuildTile - 1) / kBuildTile; }
+
+static void enqueue_cell_starts(sph_cuda *h, int *out, unsigned *occ)
+{
+    k_cell_starts<<<build_tiles_of(h), kBuildThreads, 0, h->stream>>>(
+        h->cnt, h->M, h->d_nocell, h->build_tiles, out, h->d_state, occ, h->max_bucket,
+        h->max_neighbors);
+}
+
 static const char *const kKernelNames[] = {
-    "viscosity_predict", "cell_scan_reduce_1", "cell_scan_apply_1", "cell_scatter_1",
-    "cell_permute_1",    "density",            "relax_update",       "cell_scan_reduce_2",
-    "cell_scan_apply_2", "cell_scatter_2",     "cell_permute_2"};
-static const int kStepKernels = 11;
+    "viscosity_predict", "cell_starts_1", "cell_scatter_1", "cell_permute_1", "density",
+    "relax_update",      "cell_starts_2", "cell_scatter_2", "cell_permute_2"};
+static const int kStepKernels = 9;
 // A step with a learned model: density becomes the feature pass, then the
 // network, then the relaxation with fallback.
 static const char *const kLearnedKernelNames[] = {
-    "viscosity_predict", "cell_scan_reduce_1", "cell_scan_apply_1", "cell_scatter_1",
-    "cell_permute_1",    "features",           "mlp",                "relax_learned",
-    "relax_fallback",    "cell_scan_reduce_2", "cell_scan_apply_2",  "cell_scatter_2",
-    "cell_permute_2"};
-static const int kLearnedStepKernels = 13;
+    "viscosity_predict", "cell_starts_1",  "cell_scatter_1", "cell_permute_1",
+    "features",          "mlp",            "relax_learned",  "relax_fallback",
+    "cell_starts_2",     "cell_scatter_2", "cell_permute_2"};
+static const int kLearnedStepKernels = 11;
 
-// Viscosity + prediction, the rebuild into the C order (kernels 0-4 of a step).
+// Viscosity + prediction, the rebuild into the C order (kernels 0-3 of a step).
 template <class Mark>
 static void enqueue_predict_sort(sph_cuda *h, Mark &mark)
 {
     const int n = h->n;
     const int nb = blocks_for(n);
-    const int M = h->M;
-    const int tiles = (M + kScanTile - 1) / kScanTile;
     const Ctx c = make_ctx(h);
     DevState *st = h->d_state;
     {
@@ -1077,13 +1246,10 @@ static void enqueue_predict_sort(sph_cuda *h, Mark &mark)
             &st->build_max_occ[SLOT_PREDICTED], h->pos_b, h->prev_b, h->kr_b, h->cnt, nullptr);
     }
     mark();
-    k_scan_reduce<<<tiles, kScanThreads, 0, h->stream>>>(h->cnt, M, h->d_nocell, h->tile_sums, st,
-                                                         &st->build_max_occ[SLOT_PREDICTED],
-                                                         h->max_bucket, h->max_neighbors);
+    enqueue_cell_starts(h, h->start_c, &st->build_max_occ[SLOT_PREDICTED]);
     mark();
-    k_scan_apply<<<tiles, kScanThreads, 0, h->stream>>>(h->cnt, M, h->tile_sums, h->start_c, 1);
-    mark();
-    k_scatter_ids<<<nb, kBlock, 0, h->stream>>>(n, h->kr_b, h->id_a, h->start_c, h->tmp_id);
+    k_scatter_ids<<<nb, kBlock, 0, h->stream>>>(n, h->kr_b, h->id_a, h->start_c, h->tmp_id,
+                                                h->build_tiles, build_tiles_of(h));
     mark();
     k_permute<<<nb, kBlock, 0, h->stream>>>(n, h->kr_b, h->start_c, h->tmp_id, h->id_a, h->pos_b,
                                             h->prev_b, h->id_c, h->pos_c, h->prev_c, nullptr);
@@ -1153,8 +1319,6 @@ int enqueue_step(sph_cuda *h, cudaEvent_t *events, int *nkernels)
 {
     const int n = h->n;
     const int nb = blocks_for(n);
-    const int M = h->M;
-    const int tiles = (M + kScanTile - 1) / kScanTile;
     const Ctx c = make_ctx(h);
     DevState *st = h->d_state;
     int e = 0;
@@ -1181,13 +1345,10 @@ int enqueue_step(sph_cuda *h, cudaEvent_t *events, int *nkernels)
             h->vel_b, h->kr_b, h->cnt, nullptr);
         mark();
     }
-    k_scan_reduce<<<tiles, kScanThreads, 0, h->stream>>>(h->cnt, M, h->d_nocell, h->tile_sums, st,
-                                                         &st->build_max_occ[SLOT_RELAXED],
-                                                         h->max_bucket, h->max_neighbors);
+    enqueue_cell_starts(h, h->start_a, &st->build_max_occ[SLOT_RELAXED]);
     mark();
-    k_scan_apply<<<tiles, kScanThreads, 0, h->stream>>>(h->cnt, M, h->tile_sums, h->start_a, 1);
-    mark();
-    k_scatter_ids<<<nb, kBlock, 0, h->stream>>>(n, h->kr_b, h->id_c, h->start_a, h->tmp_id);
+    k_scatter_ids<<<nb, kBlock, 0, h->stream>>>(n, h->kr_b, h->id_c, h->start_a, h->tmp_id,
+                                                h->build_tiles, build_tiles_of(h));
     mark();
     k_permute<<<nb, kBlock, 0, h->stream>>>(n, h->kr_b, h->start_a, h->tmp_id, h->id_c, h->pos_b,
                                             h->vel_b, h->id_a, h->pos_a, h->vel_a, st);
@@ -1226,7 +1387,8 @@ int upload_soa_device(sph_cuda *h, int n)
         const int rc = launch_scan(h, h->cnt, h->M, h->start_a, &st->build_max_occ[SLOT_RELAXED],
                                    true, h->d_nocell);
         if (rc != SPH_OK) return rc;
-        k_scatter_ids<<<nb, kBlock, 0, h->stream>>>(n, h->kr_b, nullptr, h->start_a, h->tmp_id);
+        k_scatter_ids<<<nb, kBlock, 0, h->stream>>>(n, h->kr_b, nullptr, h->start_a, h->tmp_id,
+                                                    nullptr, 0);
         k_permute<<<nb, kBlock, 0, h->stream>>>(n, h->kr_b, h->start_a, h->tmp_id, nullptr,
                                                 h->pos_b, h->vel_b, h->id_a, h->pos_a, h->vel_a,
                                                 nullptr);

@@ -26,7 +26,8 @@ __global__ void k_scan_reduce(const unsigned *__restrict__ in, int M,
 __global__ void k_scan_apply(unsigned *__restrict__ in, int M, const int *__restrict__ tile_sums,
                              int *__restrict__ out, int zero_input);
 __global__ void k_scatter_ids(int n, const uint2 *__restrict__ kr, const int *__restrict__ id_src,
-                              const int *__restrict__ start, int *__restrict__ tmp);
+                              const int *__restrict__ start, int *__restrict__ tmp,
+                              unsigned *tile_cnt, int ntiles);
 __global__ void k_permute(int n, const uint2 *__restrict__ kr, const int *__restrict__ start,
                           const int *__restrict__ tmp, const int *__restrict__ id_src,
                           const float2 *__restrict__ a_src, const float2 *__restrict__ b_src,
@@ -227,7 +228,7 @@ extern "C" int sph_cuda_density_static(const float *x, const float *y, int n,
     k_scan_reduce<<<nt, kScanThreads, 0, s>>>(cnt, M, nocell, tiles, state, occ, sc.max_bucket,
                                               sc.max_neighbors);
     k_scan_apply<<<nt, kScanThreads, 0, s>>>(cnt, M, tiles, start, 1);
-    k_scatter_ids<<<nb, kBlock, 0, s>>>(n, kr, nullptr, start, tmp);
+    k_scatter_ids<<<nb, kBlock, 0, s>>>(n, kr, nullptr, start, tmp, nullptr, 0);
     k_permute<<<nb, kBlock, 0, s>>>(n, kr, start, tmp, nullptr, pos_in, nullptr, id_s, pos_s,
                                     nullptr, nullptr);
     k_density<<<nb, kBlock, 0, s>>>(c, pos_s, start, occ, xr, m01, m2);

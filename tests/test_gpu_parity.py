@@ -327,5 +327,5 @@ def test_kernel_times(cuda_lib):
     with Simulation.from_scene(sc) as s:
         s.step(P, 3)
         times = s.kernel_times(P)
-        assert s.launches_per_step() == 11
-    assert len(times) == 11 and all(v > 0 for v in times.values())
+        assert s.launches_per_step() == 9
+    assert len(times) == 9 and all(v > 0 for v in times.values())
