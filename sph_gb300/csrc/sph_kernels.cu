@@ -471,34 +471,39 @@ __device__ __forceinline__ void viscosity_predict_one(
     const float sigma = __ldg(&S->P.sigma), beta = __ldg(&S->P.beta);
 
     const float2 p = pos[i];
-    float2 v = vel[i];
-    v.y = __fadd_rn(v.y, gdt);
+    const float2 v0 = vel[i];  // before gravity: velocity differences need none
+    float2 v = make_float2(v0.x, __fadd_rn(v0.y, gdt));
     float2 dv = make_float2(0.0f, 0.0f);
     const unsigned key = cell_key(p.x, p.y, g);
     // One pair's impulse on this particle; self (and any coincident
     // particle) has r2 == 0 and gives none, as u is NaN in the reference for
-    // r == 0 (fluid.c:446-451).
+    // r == 0 (fluid.c:446-451).  IN_RANGE: the caller has established
+    // r2 <= h2 (a hit-mask walk recomputes the same r2).
     const float2 mp = make_float2(-p.x, -p.y);
-    auto impulse_with = [&](const float4 &d) {
+    auto impulse_core = [&](const float4 &d, bool in_range) {
         float2 e;
         const float r2 = dist2_packed(mp, make_float2(d.x, d.y), e);
         const float qx = e.x, qy = e.y;
-        if (r2 > h2 || r2 == 0.0f) return;
-        float2 w = make_float2(d.z, d.w);
-        w.y = __fadd_rn(w.y, gdt);
+        if ((!in_range && r2 > h2) || r2 == 0.0f) return;
         const float r_recip = rsqrtf(r2);
         const float r = r2 * r_recip;
-        const float u = ((v.x - w.x) * qx + (v.y - w.y) * qy) * r_recip;
-        if (u > 0.0f) {
-            const float ratio = r * h_recip;
-            const float imp = dt * (1.0f - ratio) * (sigma * u + beta * u * u);
-            // per component imp * q * r_recip, clamped, halved and subtracted
-            // (packed FP32x2, each operation rounded as the scalar form)
-            const float2 t = __fmul2_rn(__fmul2_rn(make_float2(imp, imp), e),
-                                        make_float2(r_recip, r_recip));
-            dv = __ffma2_rn(make_float2(-0.5f, -0.5f), make_float2(clamp5(t.x), clamp5(t.y)), dv);
-        }
+        // gravity adds the same amount to both velocities: the difference
+        // is taken before it
+        const float u0 = ((v0.x - d.z) * qx + (v0.y - d.w) * qy) * r_recip;
+        // only approaching pairs (u > 0) push; the others run the same
+        // instructions with u = 0, whose impulse is +-0 and leaves dv's bits
+        // as they are (no divergent branch: about half the pairs of every
+        // warp approach)
+        const float u = u0 > 0.0f ? u0 : 0.0f;
+        const float ratio = r * h_recip;
+        const float imp = dt * (1.0f - ratio) * (sigma * u + beta * u * u);
+        // per component imp * q * r_recip, clamped, halved and subtracted
+        // (packed FP32x2, each operation rounded as the scalar form)
+        const float2 t = __fmul2_rn(__fmul2_rn(make_float2(imp, imp), e),
+                                    make_float2(r_recip, r_recip));
+        dv = __ffma2_rn(make_float2(-0.5f, -0.5f), make_float2(clamp5(t.x), clamp5(t.y)), dv);
     };
+    auto impulse_with = [&](const float4 &d) { impulse_core(d, false); };
     auto load_pv = [&](int j) {
         const float2 q = __ldg(pos + j), w = __ldg(vel + j);
         return make_float4(q.x, q.y, w.x, w.y);
@@ -540,7 +545,7 @@ __device__ __forceinline__ void viscosity_predict_one(
 #pragma unroll
                 for (int r = 0; r < 3; ++r)
                     walk_mask<float4>(m[r], ra[r], c.n, load_pv,
-                                      [&](int, const float4 &d) { impulse_with(d); });
+                                      [&](int, const float4 &d) { impulse_core(d, true); });
                 walked = true;
             }
         }
