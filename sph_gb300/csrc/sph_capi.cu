@@ -228,7 +228,7 @@ static void free_all(sph_cuda *h)
     }
     if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
     void *ptrs[] = {h->pos_a, h->vel_a, h->id_a, h->pos_b, h->prev_b, h->vel_b, h->kr_b,
-                    h->pos_c, h->prev_c, h->xr_c, h->mask01_c, h->mask2_c, h->id_c,
+                    h->pos_c, h->prev_c, h->xr_c, h->mask01_c, h->mask2_c, h->rows_c, h->id_c,
                     h->tmp_id, h->cnt, h->start_a, h->start_c, h->tile_sums, h->build_tiles, h->d_scenes,
                     h->d_p_off, h->d_nocell, h->d_state, h->d_partials, h->d_scratch};
     for (void *p : ptrs)
@@ -322,7 +322,7 @@ static int build_handle(sph_cuda **out, std::vector<Scene> &&scenes, int capacit
         (rc = dalloc(&h->pos_b, N)) || (rc = dalloc(&h->prev_b, N)) ||
         (rc = dalloc(&h->vel_b, N)) || (rc = dalloc(&h->kr_b, N)) || (rc = dalloc(&h->pos_c, N)) ||
         (rc = dalloc(&h->prev_c, N)) || (rc = dalloc(&h->xr_c, N)) ||
-        (rc = dalloc(&h->mask01_c, N)) || (rc = dalloc(&h->mask2_c, N)) ||
+        (rc = dalloc(&h->mask01_c, N)) || (rc = dalloc(&h->mask2_c, N)) || (rc = dalloc(&h->rows_c, N)) ||
         (rc = dalloc(&h->id_c, N)) || (rc = dalloc(&h->tmp_id, N)) ||
         (rc = dalloc(&h->cnt, std::max(M, N + 1))) ||
         (rc = dalloc(&h->start_a, std::max(M + 1, N + 1))) || (rc = dalloc(&h->start_c, M + 1)) ||

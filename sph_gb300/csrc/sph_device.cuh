@@ -251,6 +251,13 @@ __device__ __forceinline__ void stencil_rows(unsigned key, const int *__restrict
 
 constexpr int kMaskRow = 64;  // candidates per stencil row recorded in a hit mask
 
+// What a density pass leaves for the relaxation of the same positions, per
+// particle: the first slot of each stencil row (x, y, z) and how to walk
+// (w): kRowsNone, no neighbours (out of the grid or beyond the bucket cap);
+// kRowsMasked, walk the hit masks from those slots; kRowsFull, search the
+// whole stencil again (a row longer than kMaskRow, or an overflowing bucket).
+constexpr int kRowsNone = 0, kRowsMasked = 1, kRowsFull = 2;
+
 // Visits the set bits of a 64-bit row mask in increasing order with one
 // neighbour's data in flight: load(j) for slot base + t of the next bit is
 // issued before visit(j, data) runs on the previous one, so the loads of a

@@ -117,6 +117,7 @@ struct sph_cuda {
     float4 *xr_c = nullptr;               // (x, y, rho, rho_near) of the density pass
     ulonglong2 *mask01_c = nullptr;       // neighbour hit masks of stencil rows 0, 1
     unsigned long long *mask2_c = nullptr;  // ... and row 2
+    int4 *rows_c = nullptr;               // the stencil rows' first slots and walk mode
     int *id_c = nullptr;
     int *tmp_id = nullptr;
     unsigned int *cnt = nullptr;  // M counters, zero between builds

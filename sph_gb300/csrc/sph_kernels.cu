@@ -608,7 +608,8 @@ __device__ __forceinline__ void density_one(int i, const Ctx &c, const float2 *_
                                             const int *__restrict__ start, bool capped,
                                             float4 *__restrict__ xr_out,
                                             ulonglong2 *__restrict__ mask01,
-                                            unsigned long long *__restrict__ mask2)
+                                            unsigned long long *__restrict__ mask2,
+                                            int4 *__restrict__ rows_out)
 {
     const Scene *S = c.scenes + scene_of(c, i);
     const SG g = load_grid(S);
@@ -620,10 +621,14 @@ __device__ __forceinline__ void density_one(int i, const Ctx &c, const float2 *_
     const unsigned key = cell_key(p.x, p.y, g);
     float a = 0.0f, b = 0.0f;
     unsigned long long m[3] = {0ull, 0ull, 0ull};
+    int4 rec = make_int4(0, 0, 0, kRowsNone);
     if (searchable(key, i, start, g, capped, c.max_bucket)) {
+        rec.w = kRowsFull;
         if (!capped) {
             int ra[3], rl[3];
             stencil_rows(key, start, g, ra, rl, c.n);
+            if (rl[0] <= kMaskRow && rl[1] <= kMaskRow && rl[2] <= kMaskRow)
+                rec = make_int4(ra[0], ra[1], ra[2], kRowsMasked);
 #pragma unroll
             for (int r = 0; r < 3; ++r) {
                 const float2 *row = pos + ra[r];
@@ -692,33 +697,36 @@ __device__ __forceinline__ void density_one(int i, const Ctx &c, const float2 *_
     xr_out[i] = make_float4(p.x, p.y, a, b);
     mask01[i] = make_ulonglong2(m[0], m[1]);
     mask2[i] = m[2];
+    if (rows_out) rows_out[i] = rec;
 }
 
 template <bool PERSIST>
 __global__ void __launch_bounds__(kMaxBlock)
 k_density_t(Ctx c, const float2 *__restrict__ pos, const int *__restrict__ start,
             const unsigned *__restrict__ occ_in, float4 *__restrict__ xr_out,
-            ulonglong2 *__restrict__ mask01, unsigned long long *__restrict__ mask2)
+            ulonglong2 *__restrict__ mask01, unsigned long long *__restrict__ mask2,
+            int4 *__restrict__ rows_out)
 {
     const bool capped = *occ_in > (unsigned)c.max_bucket;
     const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
     if (!PERSIST) {
-        if (i0 < c.n) density_one(i0, c, pos, start, capped, xr_out, mask01, mask2);
+        if (i0 < c.n) density_one(i0, c, pos, start, capped, xr_out, mask01, mask2, rows_out);
         return;
     }
     for (int i = i0; i < c.n; i += gridDim.x * blockDim.x)
-        density_one(i, c, pos, start, capped, xr_out, mask01, mask2);
+        density_one(i, c, pos, start, capped, xr_out, mask01, mask2, rows_out);
 }
 
 // One density launch per block (the form other translation units call).
 __global__ void __launch_bounds__(kMaxBlock)
 k_density(Ctx c, const float2 *__restrict__ pos, const int *__restrict__ start,
           const unsigned *__restrict__ occ_in, float4 *__restrict__ xr_out,
-          ulonglong2 *__restrict__ mask01, unsigned long long *__restrict__ mask2)
+          ulonglong2 *__restrict__ mask01, unsigned long long *__restrict__ mask2,
+          int4 *__restrict__ rows_out)
 {
     const bool capped = *occ_in > (unsigned)c.max_bucket;
     const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i0 < c.n) density_one(i0, c, pos, start, capped, xr_out, mask01, mask2);
+    if (i0 < c.n) density_one(i0, c, pos, start, capped, xr_out, mask01, mask2, rows_out);
 }
 
 // ---------------------------------------------------------------------------
@@ -811,11 +819,11 @@ struct LearnedIn {
 template <bool PROBE, bool LEARNED = false>
 __device__ __forceinline__ void relax_update_one(
     int i, const Ctx &cx, const float4 *__restrict__ xr, const ulonglong2 *__restrict__ mask01,
-    const unsigned long long *__restrict__ mask2, const float2 *__restrict__ prev,
-    const int *__restrict__ ids, const int *__restrict__ start, bool capped,
-    float2 *__restrict__ pos_out, float2 *__restrict__ vel_out, uint2 *__restrict__ kr_out,
-    unsigned *__restrict__ cnt, float2 *__restrict__ probe_out, const LearnedIn &L = LearnedIn(),
-    bool *used_net = nullptr)
+    const unsigned long long *__restrict__ mask2, const int4 *__restrict__ rows,
+    const float2 *__restrict__ prev, const int *__restrict__ ids, const int *__restrict__ start,
+    bool capped, float2 *__restrict__ pos_out, float2 *__restrict__ vel_out,
+    uint2 *__restrict__ kr_out, unsigned *__restrict__ cnt, float2 *__restrict__ probe_out,
+    const LearnedIn &L = LearnedIn(), bool *used_net = nullptr)
 {
     const Scene *S = cx.scenes + scene_of(cx, i);
     const SG g = load_grid(S);
@@ -833,7 +841,6 @@ __device__ __forceinline__ void relax_update_one(
     const float4 me = xr[i];
     const float2 p = make_float2(me.x, me.y);
     const float Pi = c.k * (me.z - c.rest), Pni = c.k_near * me.w;
-    const unsigned key = cell_key(p.x, p.y, g);
     // constants of the masked walk, pre-multiplied by dt^2 (fewer live values)
     WalkConsts wc;
     wc.h_recip = c.h_recip;
@@ -856,32 +863,44 @@ __device__ __forceinline__ void relax_update_one(
     }
     if (LEARNED && used_net) *used_net = net;
     if (LEARNED && !net && L.defer) return;
-    if (!net && searchable(key, i, start, g, capped, cx.max_bucket)) {
-        bool walked = false;
-        if (!capped) {
-            int ra[3], rl[3];
+    // the density pass's row record: the stencil rows' first slots, so the
+    // walk needs neither the cell key nor the cell starts (without one, the
+    // rows are found here)
+    int mode = net ? kRowsNone : kRowsFull;
+    int ra[3] = {0, 0, 0};
+    if (!net && rows) {
+        const int4 rw = __ldg(rows + i);
+        mode = rw.w;
+        ra[0] = rw.x; ra[1] = rw.y; ra[2] = rw.z;
+    }
+    unsigned key = 0u;
+    if (mode == kRowsFull) {
+        key = cell_key(p.x, p.y, g);
+        if (!searchable(key, i, start, g, capped, cx.max_bucket)) {
+            mode = kRowsNone;
+        } else if (!capped) {
+            int rl[3];
             stencil_rows(key, start, g, ra, rl, cx.n);
-            if (rl[0] <= kMaskRow && rl[1] <= kMaskRow && rl[2] <= kMaskRow) {
-                const ulonglong2 m01 = mask01[i];
-                const unsigned long long mm[3] = {m01.x, m01.y, mask2[i]};
+            if (rl[0] <= kMaskRow && rl[1] <= kMaskRow && rl[2] <= kMaskRow) mode = kRowsMasked;
+        }
+    }
+    if (mode == kRowsMasked) {
+        const ulonglong2 m01 = mask01[i];
+        const unsigned long long mm[3] = {m01.x, m01.y, mask2[i]};
 #pragma unroll
-                for (int r = 0; r < 3; ++r)
-                    walk_mask<float4>(
-                        mm[r], ra[r], cx.n, [&](int j) { return __ldg(xr + j); },
-                        [&](int j, const float4 &q) {
-                            relax_pair_walk(wc, p, q, i, j, S, ids, acc, nudges);
-                        });
-                walked = true;
-            }
-        }
-        if (!walked) {
-            for_each_candidate(key, start, g, capped, cx.max_bucket, cx.n, [&](int j) {
-                if (j == i) return;
-                const float4 q = __ldg(xr + j);
-                if (dist2(p.x - q.x, p.y - q.y) > c.h2) return;
-                relax_pair_walk(wc, p, q, i, j, S, ids, acc, nudges);
-            });
-        }
+        for (int r = 0; r < 3; ++r)
+            walk_mask<float4>(
+                mm[r], ra[r], cx.n, [&](int j) { return __ldg(xr + j); },
+                [&](int j, const float4 &q) {
+                    relax_pair_walk(wc, p, q, i, j, S, ids, acc, nudges);
+                });
+    } else if (mode == kRowsFull) {
+        for_each_candidate(key, start, g, capped, cx.max_bucket, cx.n, [&](int j) {
+            if (j == i) return;
+            const float4 q = __ldg(xr + j);
+            if (dist2(p.x - q.x, p.y - q.y) > c.h2) return;
+            relax_pair_walk(wc, p, q, i, j, S, ids, acc, nudges);
+        });
     }
     const float nd = (float)nudges * 0.000001f;
     if (PROBE) {
@@ -909,7 +928,8 @@ __device__ __forceinline__ void relax_update_one(
 template <bool PROBE, bool PERSIST = false>
 __global__ void __launch_bounds__(kBlock, SPH_RELAX_MIN_BLOCKS)
 k_relax_update(Ctx c, const float4 *__restrict__ xr, const ulonglong2 *__restrict__ mask01,
-               const unsigned long long *__restrict__ mask2, const float2 *__restrict__ prev,
+               const unsigned long long *__restrict__ mask2, const int4 *__restrict__ rows,
+               const float2 *__restrict__ prev,
                const int *__restrict__ ids, const int *__restrict__ start,
                const unsigned *__restrict__ occ_in, unsigned *occ_reset,
                float2 *__restrict__ pos_out, float2 *__restrict__ vel_out,
@@ -921,12 +941,12 @@ k_relax_update(Ctx c, const float4 *__restrict__ xr, const ulonglong2 *__restric
     const bool capped = *occ_in > (unsigned)c.max_bucket;
     if (!PERSIST) {
         if (i0 < c.n)
-            relax_update_one<PROBE>(i0, c, xr, mask01, mask2, prev, ids, start, capped, pos_out,
+            relax_update_one<PROBE>(i0, c, xr, mask01, mask2, rows, prev, ids, start, capped, pos_out,
                                     vel_out, kr_out, cnt, probe_out);
         return;
     }
     for (int i = i0; i < c.n; i += gridDim.x * blockDim.x)
-        relax_update_one<PROBE>(i, c, xr, mask01, mask2, prev, ids, start, capped, pos_out,
+        relax_update_one<PROBE>(i, c, xr, mask01, mask2, rows, prev, ids, start, capped, pos_out,
                                 vel_out, kr_out, cnt, probe_out);
 }
 
@@ -938,7 +958,8 @@ k_relax_update(Ctx c, const float4 *__restrict__ xr, const ulonglong2 *__restric
 template <bool PROBE>
 __global__ void __launch_bounds__(kBlock, 4)
 k_relax_learned(Ctx c, const float4 *__restrict__ xr, const ulonglong2 *__restrict__ mask01,
-                const unsigned long long *__restrict__ mask2, const float2 *__restrict__ prev,
+                const unsigned long long *__restrict__ mask2, const int4 *__restrict__ rows,
+                const float2 *__restrict__ prev,
                 const int *__restrict__ ids, const int *__restrict__ start,
                 const unsigned *__restrict__ occ_in, unsigned *occ_reset,
                 float2 *__restrict__ pos_out, float2 *__restrict__ vel_out,
@@ -954,7 +975,7 @@ k_relax_learned(Ctx c, const float4 *__restrict__ xr, const ulonglong2 *__restri
     bool used = true;
     L.defer = !PROBE;
     if (i < c.n)
-        relax_update_one<PROBE, true>(i, c, xr, mask01, mask2, prev, ids, start, capped, pos_out,
+        relax_update_one<PROBE, true>(i, c, xr, mask01, mask2, rows, prev, ids, start, capped, pos_out,
                                       vel_out, kr_out, cnt, probe_out, L, &used);
     if (PROBE) return;
     const unsigned fb = __ballot_sync(0xffffffffu, !used);
@@ -972,7 +993,8 @@ k_relax_learned(Ctx c, const float4 *__restrict__ xr, const ulonglong2 *__restri
 // only).  Block 0 adds the count to the fallback statistics.
 __global__ void __launch_bounds__(kBlock, 4)
 k_relax_fallback(Ctx c, const float4 *__restrict__ xr, const ulonglong2 *__restrict__ mask01,
-                 const unsigned long long *__restrict__ mask2, const float2 *__restrict__ prev,
+                 const unsigned long long *__restrict__ mask2, const int4 *__restrict__ rows,
+                 const float2 *__restrict__ prev,
                  const int *__restrict__ ids, const int *__restrict__ start,
                  const unsigned *__restrict__ occ_in, float2 *__restrict__ pos_out,
                  float2 *__restrict__ vel_out, uint2 *__restrict__ kr_out,
@@ -983,7 +1005,7 @@ k_relax_fallback(Ctx c, const float4 *__restrict__ xr, const ulonglong2 *__restr
     if (t0 == 0) atomicAdd(&st->learned_fallback, (unsigned long long)total);
     const bool capped = *occ_in > (unsigned)c.max_bucket;
     for (unsigned k = t0; k < total; k += gridDim.x * blockDim.x)
-        relax_update_one<false>(fb_list[k], c, xr, mask01, mask2, prev, ids, start, capped,
+        relax_update_one<false>(fb_list[k], c, xr, mask01, mask2, rows, prev, ids, start, capped,
                                 pos_out, vel_out, kr_out, cnt, nullptr);
 }
 
@@ -1267,7 +1289,7 @@ static void enqueue_density(sph_cuda *h)
     auto kd = h->shape[1].persistent ? k_density_t<true> : k_density_t<false>;
     kd<<<gather_grid(h, h->shape[1]), h->shape[1].block, 0, h->stream>>>(
         make_ctx(h), h->pos_c, h->start_c, &st->build_max_occ[SLOT_PREDICTED], h->xr_c,
-        h->mask01_c, h->mask2_c);
+        h->mask01_c, h->mask2_c, h->rows_c);
 }
 
 // The C-order state of the next step's relaxation -- predicted positions,
@@ -1301,19 +1323,19 @@ int launch_learned_relax(sph_cuda *h, float2 *probe_out, cudaEvent_t *events)
     const unsigned *occ = &st->build_max_occ[SLOT_PREDICTED];
     if (probe_out) {
         k_relax_learned<true><<<nb, kBlock, 0, h->stream>>>(
-            c, h->xr_c, h->mask01_c, h->mask2_c, h->prev_c, h->id_c, h->start_c, occ, nullptr,
-            nullptr, nullptr, nullptr, nullptr, probe_out, L, st, nullptr);
+            c, h->xr_c, h->mask01_c, h->mask2_c, h->rows_c, h->prev_c, h->id_c, h->start_c, occ,
+            nullptr, nullptr, nullptr, nullptr, nullptr, probe_out, L, st, nullptr);
         return cuda_fail(cudaGetLastError(), "learned relaxation probe");
     }
     k_relax_learned<false><<<nb, kBlock, 0, h->stream>>>(
-        c, h->xr_c, h->mask01_c, h->mask2_c, h->prev_c, h->id_c, h->start_c, occ,
+        c, h->xr_c, h->mask01_c, h->mask2_c, h->rows_c, h->prev_c, h->id_c, h->start_c, occ,
         &st->build_max_occ[SLOT_RELAXED], h->pos_b, h->vel_b, h->kr_b, h->cnt, nullptr, L, st,
         h->fb_list);
     if (events) cudaEventRecord(events[0], h->stream);
     const int fb_blocks = std::min(nb, 4 * h->num_sms);
     k_relax_fallback<<<fb_blocks, kBlock, 0, h->stream>>>(
-        c, h->xr_c, h->mask01_c, h->mask2_c, h->prev_c, h->id_c, h->start_c, occ, h->pos_b,
-        h->vel_b, h->kr_b, h->cnt, st, h->fb_list);
+        c, h->xr_c, h->mask01_c, h->mask2_c, h->rows_c, h->prev_c, h->id_c, h->start_c, occ,
+        h->pos_b, h->vel_b, h->kr_b, h->cnt, st, h->fb_list);
     if (events) cudaEventRecord(events[1], h->stream);
     return cuda_fail(cudaGetLastError(), "learned relaxation");
 }
@@ -1345,7 +1367,7 @@ int enqueue_step(sph_cuda *h, cudaEvent_t *events, int *nkernels)
         mark();
         auto kr = h->shape[2].persistent ? k_relax_update<false, true> : k_relax_update<false, false>;
         kr<<<gather_grid(h, h->shape[2]), h->shape[2].block, 0, h->stream>>>(
-            c, h->xr_c, h->mask01_c, h->mask2_c, h->prev_c, h->id_c, h->start_c,
+            c, h->xr_c, h->mask01_c, h->mask2_c, h->rows_c, h->prev_c, h->id_c, h->start_c,
             &st->build_max_occ[SLOT_PREDICTED], &st->build_max_occ[SLOT_RELAXED], h->pos_b,
             h->vel_b, h->kr_b, h->cnt, nullptr);
         mark();
@@ -1438,7 +1460,7 @@ int launch_scene_diagnostics(sph_cuda *h, double *d_out)
 size_t probe_scratch_bytes(int n)
 {
     const size_t a = ((size_t)n * 16 + 255) & ~(size_t)255;
-    return 3 * a + (((size_t)n * 8 + 255) & ~(size_t)255);
+    return 4 * a + (((size_t)n * 8 + 255) & ~(size_t)255);
 }
 
 int launch_probe(sph_cuda *h, int which, void *scratch, float2 *out)
@@ -1454,12 +1476,13 @@ int launch_probe(sph_cuda *h, int which, void *scratch, float2 *out)
     float4 *xr = (float4 *)base;
     ulonglong2 *m01 = (ulonglong2 *)(base + a);
     unsigned long long *m2 = (unsigned long long *)(base + 2 * a);
-    float2 *sorted = (float2 *)(base + 3 * a);
+    int4 *rw = (int4 *)(base + 3 * a);
+    float2 *sorted = (float2 *)(base + 4 * a);
     if (which == 0 || which == 1) {
-        k_density<<<nb, kBlock, 0, h->stream>>>(c, h->pos_a, h->start_a, occ, xr, m01, m2);
+        k_density<<<nb, kBlock, 0, h->stream>>>(c, h->pos_a, h->start_a, occ, xr, m01, m2, rw);
         if (which == 1)
             k_relax_update<true><<<nb, kBlock, 0, h->stream>>>(
-                c, xr, m01, m2, nullptr, h->id_a, h->start_a, occ, nullptr, nullptr, nullptr,
+                c, xr, m01, m2, rw, nullptr, h->id_a, h->start_a, occ, nullptr, nullptr, nullptr,
                 nullptr, nullptr, sorted);
         else
             k_xr_density<<<nb, kBlock, 0, h->stream>>>(n, xr, sorted);

@@ -83,7 +83,8 @@ __global__ void __launch_bounds__(kBlock)
 k_features(Ctx c, const float2 *__restrict__ pos, const float2 *__restrict__ prev,
            const int *__restrict__ start, const unsigned *__restrict__ occ_in,
            float4 *__restrict__ xr_out, ulonglong2 *__restrict__ mask01,
-           unsigned long long *__restrict__ mask2, __nv_bfloat16 *__restrict__ feat,
+           unsigned long long *__restrict__ mask2, int4 *__restrict__ rows_out,
+           __nv_bfloat16 *__restrict__ feat,
            unsigned short *__restrict__ nbcount, unsigned *__restrict__ fb_count)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -109,10 +110,14 @@ k_features(Ctx c, const float2 *__restrict__ pos, const float2 *__restrict__ pre
     float Ms = 0.0f, Txy = 0.0f;
     int count = 0;
     bool degenerate = false;
+    int4 rec = make_int4(0, 0, 0, kRowsNone);  // as density_one's
     if (searchable(key, i, start, g, capped, c.max_bucket)) {
+        rec.w = kRowsFull;
         if (!capped) {
             int ra[3], rl[3];
             stencil_rows(key, start, g, ra, rl, c.n);
+            if (rl[0] <= kMaskRow && rl[1] <= kMaskRow && rl[2] <= kMaskRow)
+                rec = make_int4(ra[0], ra[1], ra[2], kRowsMasked);
 #pragma unroll
             for (int r = 0; r < 3; ++r) {
                 const float2 *row = pos + ra[r];
@@ -179,6 +184,7 @@ k_features(Ctx c, const float2 *__restrict__ pos, const float2 *__restrict__ pre
     xr_out[i] = make_float4(p.x, p.y, a, b);
     mask01[i] = make_ulonglong2(m[0], m[1]);
     mask2[i] = m[2];
+    rows_out[i] = rec;
     nbcount[i] = degenerate ? (unsigned short)65535 : (unsigned short)(count < 65534 ? count : 65534);
     const float V1x = V1.x, V1y = V1.y, V2x = V2.x, V2y = V2.y;
     const float Txx = Tdiag.x, Tyy = Tdiag.y;
@@ -984,7 +990,7 @@ int launch_features(sph_cuda *h, __nv_bfloat16 *feat, unsigned short *nbc)
     if (h->n == 0) return SPH_OK;
     ml::k_features<<<nblk(h->n), kBlock, 0, h->stream>>>(
         make_ctx(h), h->pos_c, h->prev_c, h->start_c, &h->d_state->build_max_occ[SLOT_PREDICTED],
-        h->xr_c, h->mask01_c, h->mask2_c, feat, nbc, &h->d_state->fb_count);
+        h->xr_c, h->mask01_c, h->mask2_c, h->rows_c, feat, nbc, &h->d_state->fb_count);
     return cuda_fail(cudaGetLastError(), "features");
 }
 

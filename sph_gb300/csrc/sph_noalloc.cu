@@ -35,7 +35,8 @@ __global__ void k_permute(int n, const uint2 *__restrict__ kr, const int *__rest
                           float2 *__restrict__ b_dst, DevState *__restrict__ end_step);
 __global__ void k_density(Ctx c, const float2 *__restrict__ pos, const int *__restrict__ start,
                           const unsigned *__restrict__ occ_in, float4 *__restrict__ xr_out,
-                          ulonglong2 *__restrict__ mask01, unsigned long long *__restrict__ mask2);
+                          ulonglong2 *__restrict__ mask01, unsigned long long *__restrict__ mask2,
+                          int4 *__restrict__ rows_out);
 
 namespace {
 
@@ -231,7 +232,7 @@ extern "C" int sph_cuda_density_static(const float *x, const float *y, int n,
     k_scatter_ids<<<nb, kBlock, 0, s>>>(n, kr, nullptr, start, tmp, nullptr, 0);
     k_permute<<<nb, kBlock, 0, s>>>(n, kr, start, tmp, nullptr, pos_in, nullptr, id_s, pos_s,
                                     nullptr, nullptr);
-    k_density<<<nb, kBlock, 0, s>>>(c, pos_s, start, occ, xr, m01, m2);
+    k_density<<<nb, kBlock, 0, s>>>(c, pos_s, start, occ, xr, m01, m2, nullptr);
     k_static_scatter<<<nb, kBlock, 0, s>>>(n, id_s, xr, density, density_near);
     return cuda_fail(cudaGetLastError(), "sph_cuda_density_static launch");
 }
