@@ -64,17 +64,72 @@ __device__ __forceinline__ unsigned warp_max(unsigned v)
     return v;
 }
 
-// Counts one particle with cell key `key` into its scan tile: the lanes of
+// Counts one particle with cell key `key` into its build tile: the lanes of
 // the warp that reach this call together and share a tile add with one
-// atomic (the particles of a warp are neighbours in cell order, so most
-// warps issue one or two).
+// atomic (the particles of a warp are neighbours in cell order, so almost
+// every warp issues one).
 __device__ __forceinline__ void add_tile_count(unsigned *tile_cnt, unsigned key)
 {
     if (!tile_cnt) return;
     const unsigned active = __activemask();
     const unsigned t = key / (unsigned)kBuildTile;
+    const unsigned lane = threadIdx.x & 31;
+    const int first = __ffs(active) - 1;
+    // nearly every warp's particles share one tile: a broadcast and a vote
+    // settle it; the rest group their lanes by tile
+    const unsigned t0 = __shfl_sync(active, t, first);
+    if (__all_sync(active, t == t0)) {
+        if (lane == (unsigned)first) atomicAdd(tile_cnt + t0, (unsigned)__popc(active));
+        return;
+    }
     const unsigned peers = __match_any_sync(active, t);
-    if ((threadIdx.x & 31) == (unsigned)(__ffs(peers) - 1)) atomicAdd(tile_cnt + t, (unsigned)__popc(peers));
+    if (lane == (unsigned)(__ffs(peers) - 1)) atomicAdd(tile_cnt + t, (unsigned)__popc(peers));
+}
+
+// The same count for a whole CTA, called once by every thread of it (t: the
+// build tile of the key the thread made, -1 for none): warps whose keys
+// share one tile report it to thread 0, which adds runs of equal tiles with
+// one atomic each.  The particles a CTA advances lie in one or two tiles,
+// and the CTAs running at any moment in a narrow range of them: in a light
+// kernel (the learned relaxation) one atomic per warp makes those few
+// counters a hot spot, one per CTA does not.  The gathers keep the warp
+// form: the barrier here would hold each CTA until its slowest warp.
+__device__ __forceinline__ void cta_tile_count(unsigned *tile_cnt, int t)
+{
+    __shared__ int s_t[kMaxBlock / 32];
+    __shared__ unsigned s_c[kMaxBlock / 32];
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned made = __ballot_sync(0xffffffffu, t >= 0);
+    int t0 = -1;
+    bool uniform = true;
+    if (made) {
+        t0 = __shfl_sync(0xffffffffu, t, __ffs(made) - 1);
+        uniform = __all_sync(0xffffffffu, t < 0 || t == t0);
+    }
+    if (!uniform && t >= 0) {
+        const unsigned peers = __match_any_sync(made, t);
+        if (lane == (unsigned)(__ffs(peers) - 1)) atomicAdd(tile_cnt + t, (unsigned)__popc(peers));
+    }
+    if (lane == 0) {
+        s_t[warp] = (made && uniform) ? t0 : -1;
+        s_c[warp] = (unsigned)__popc(made);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int cur = -1;
+        unsigned acc = 0u;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+            const int tw = s_t[w];
+            if (tw < 0) continue;
+            if (tw != cur) {
+                if (cur >= 0) atomicAdd(tile_cnt + cur, acc);
+                cur = tw;
+                acc = 0u;
+            }
+            acc += s_c[w];
+        }
+        if (cur >= 0) atomicAdd(tile_cnt + cur, acc);
+    }
 }
 
 // Exclusive scan over the block; returns the thread's exclusive prefix and
@@ -459,7 +514,7 @@ __device__ __forceinline__ void viscosity_predict_one(
     int i, const Ctx &c, const DevState *__restrict__ st, const float2 *__restrict__ pos,
     const float2 *__restrict__ vel, const int *__restrict__ start, bool capped,
     float2 *__restrict__ pos_out, float2 *__restrict__ prev_out, uint2 *__restrict__ kr_out,
-    unsigned *__restrict__ cnt, float2 *__restrict__ probe_out)
+    unsigned *__restrict__ cnt, float2 *__restrict__ probe_out, int *tile_made = nullptr)
 {
     const Scene *S = c.scenes + scene_of(c, i);
     const SG g = load_grid(S);
@@ -564,7 +619,10 @@ __device__ __forceinline__ void viscosity_predict_one(
     unsigned rank = 0u;
     if (in_bounds(k2, c.M, kBadKey)) {
         rank = atomicAdd(cnt + k2, 1u);
-        add_tile_count(c.tile_cnt, k2);
+        if (tile_made)
+            *tile_made = (int)(k2 / (unsigned)kBuildTile);
+        else
+            add_tile_count(c.tile_cnt, k2);
     }
     pos_out[i] = make_float2(nx, ny);
     prev_out[i] = p;
@@ -823,7 +881,7 @@ __device__ __forceinline__ void relax_update_one(
     const float2 *__restrict__ prev, const int *__restrict__ ids, const int *__restrict__ start,
     bool capped, float2 *__restrict__ pos_out, float2 *__restrict__ vel_out,
     uint2 *__restrict__ kr_out, unsigned *__restrict__ cnt, float2 *__restrict__ probe_out,
-    const LearnedIn &L = LearnedIn(), bool *used_net = nullptr)
+    const LearnedIn &L = LearnedIn(), bool *used_net = nullptr, int *tile_made = nullptr)
 {
     const Scene *S = cx.scenes + scene_of(cx, i);
     const SG g = load_grid(S);
@@ -918,7 +976,10 @@ __device__ __forceinline__ void relax_update_one(
     unsigned rank = 0u;
     if (in_bounds(k2, cx.M, kBadKey)) {
         rank = atomicAdd(cnt + k2, 1u);
-        add_tile_count(cx.tile_cnt, k2);
+        if (tile_made)
+            *tile_made = (int)(k2 / (unsigned)kBuildTile);
+        else
+            add_tile_count(cx.tile_cnt, k2);
     }
     pos_out[i] = make_float2(nx, ny);
     vel_out[i] = make_float2(vx, vy);
@@ -974,10 +1035,12 @@ k_relax_learned(Ctx c, const float4 *__restrict__ xr, const ulonglong2 *__restri
     const bool capped = *occ_in > (unsigned)c.max_bucket;
     bool used = true;
     L.defer = !PROBE;
+    int t = -1;
     if (i < c.n)
         relax_update_one<PROBE, true>(i, c, xr, mask01, mask2, rows, prev, ids, start, capped, pos_out,
-                                      vel_out, kr_out, cnt, probe_out, L, &used);
+                                      vel_out, kr_out, cnt, probe_out, L, &used, &t);
     if (PROBE) return;
+    if (c.tile_cnt) cta_tile_count(c.tile_cnt, t);
     const unsigned fb = __ballot_sync(0xffffffffu, !used);
     if (fb) {
         const int lane = threadIdx.x & 31, leader = __ffs(fb) - 1;
