@@ -1471,6 +1471,9 @@ int upload_soa_device(sph_cuda *h, int n)
     const int nb = blocks_for(n);
     DevState *st = h->d_state;
     if (n > 0) {
+        // a fresh state starts every step's build from zero tile counts,
+        // whatever an interrupted step left
+        cudaMemsetAsync(h->build_tiles, 0, (size_t)h->ntiles * sizeof(unsigned), h->stream);
         k_iota<<<nb, kBlock, 0, h->stream>>>(n, h->id_c);
         k_keys<<<nb, kBlock, 0, h->stream>>>(make_ctx(h), h->pos_b, h->kr_b, h->cnt,
                                              &st->build_max_occ[SLOT_RELAXED]);
