@@ -116,48 +116,77 @@ k_features(Ctx c, const float2 *__restrict__ pos, const float2 *__restrict__ pre
         if (!capped) {
             int ra[3], rl[3];
             stencil_rows(key, start, g, ra, rl, c.n);
-            if (rl[0] <= kMaskRow && rl[1] <= kMaskRow && rl[2] <= kMaskRow)
-                rec = make_int4(ra[0], ra[1], ra[2], kRowsMasked);
-#pragma unroll
-            for (int r = 0; r < 3; ++r) {
-                const float2 *row = pos + ra[r];
-                unsigned long long mr = 0ull;
-                for (int t = 0; t < rl[r]; ++t) {
-                    const float2 q = __ldg(row + t);
-                    float2 e;  // q - p
-                    const float r2 = dist2_packed(mp, q, e);
-                    const float ex = e.x, ey = e.y;
-                    if (r2 <= h2) {
-                        mr |= 1ull << (t & 63);
-                        const float rinv = rsqrtf(r2);
-                        const float rr = r2 > 0.0f ? r2 * rinv : 0.0f;
-                        const float ratio = __fmul_rn(rr, h_recip);
-                        const bool other = ra[r] + t != i;
-                        count += other ? 1 : 0;
-                        degenerate |= other && r2 <= 2e-12f;
-                        if (ratio < 1.0f) {
-                            const float omr = 1.0f - ratio;
-                            const float omr2 = omr * omr;
-                            a += omr2;
-                            b += omr2 * omr;
-                            if (other) {
-                                // message sums in packed FP32x2 arithmetic
-                                const float2 u = __fmul2_rn(e, make_float2(rinv, rinv));
-                                const float2 w2 = make_float2(omr, omr);
-                                const float2 wu = __fmul2_rn(w2, u);
-                                V1 = __fadd2_rn(V1, wu);
-                                V2 = __ffma2_rn(make_float2(omr2, omr2), u, V2);
-                                Ms += omr;
-                                Tdiag = __ffma2_rn(wu, u, Tdiag);
-                                Txy += wu.x * u.y;
-                                // sum w (x_j - x_prev_j); the velocities follow at the end
-                                const float2 qp = __ldg(prev + ra[r] + t);
-                                Dsum = __ffma2_rn(w2, __fadd2_rn(q, make_float2(-qp.x, -qp.y)), Dsum);
-                            }
-                        }
+            // one neighbour's terms: density, messages, counts (self
+            // included in a and b, removed below)
+            auto visit = [&](int j, const float2 &q) {
+                float2 e;  // q - p
+                const float r2 = dist2_packed(mp, q, e);
+                const float rinv = rsqrtf(r2);
+                const float rr = r2 > 0.0f ? r2 * rinv : 0.0f;
+                const float ratio = __fmul_rn(rr, h_recip);
+                const bool other = j != i;
+                count += other ? 1 : 0;
+                degenerate |= other && r2 <= 2e-12f;
+                if (ratio < 1.0f) {
+                    const float omr = 1.0f - ratio;
+                    const float omr2 = omr * omr;
+                    a += omr2;
+                    b += omr2 * omr;
+                    if (other) {
+                        // message sums in packed FP32x2 arithmetic
+                        const float2 u = __fmul2_rn(e, make_float2(rinv, rinv));
+                        const float2 w2 = make_float2(omr, omr);
+                        const float2 wu = __fmul2_rn(w2, u);
+                        V1 = __fadd2_rn(V1, wu);
+                        V2 = __ffma2_rn(make_float2(omr2, omr2), u, V2);
+                        Ms += omr;
+                        Tdiag = __ffma2_rn(wu, u, Tdiag);
+                        Txy += wu.x * u.y;
+                        // sum w (x_j - x_prev_j); the velocities follow at the end
+                        const float2 qp = __ldg(prev + j);
+                        Dsum = __ffma2_rn(w2, __fadd2_rn(q, make_float2(-qp.x, -qp.y)), Dsum);
                     }
                 }
-                m[r] = mr;
+            };
+            if (rl[0] <= kMaskRow && rl[1] <= kMaskRow && rl[2] <= kMaskRow) {
+                rec = make_int4(ra[0], ra[1], ra[2], kRowsMasked);
+                // two phases, as the viscosity: the rows' hit masks from a
+                // cheap filter, then the heavy terms for the hits only, in
+                // the same (slot) order
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+                    const float2 *row = pos + ra[r];
+                    const int len = rl[r];
+                    unsigned lo = 0u, hi = 0u;
+                    const int n0 = min(len, 32);
+                    for (int t = 0; t < n0; ++t) {
+                        float2 e;
+                        lo |= (unsigned)(dist2_packed(mp, __ldg(row + t), e) <= h2) << t;
+                    }
+                    for (int t = 32; t < len; ++t) {
+                        float2 e;
+                        hi |= (unsigned)(dist2_packed(mp, __ldg(row + t), e) <= h2) << (t - 32);
+                    }
+                    m[r] = ((unsigned long long)hi << 32) | lo;
+                }
+#pragma unroll
+                for (int r = 0; r < 3; ++r)
+                    walk_mask<float2>(m[r], ra[r], c.n, [&](int j) { return __ldg(pos + j); }, visit);
+            } else {
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+                    const float2 *row = pos + ra[r];
+                    unsigned long long mr = 0ull;
+                    for (int t = 0; t < rl[r]; ++t) {
+                        const float2 q = __ldg(row + t);
+                        float2 e;
+                        if (dist2_packed(mp, q, e) <= h2) {
+                            mr |= 1ull << (t & 63);
+                            visit(ra[r] + t, q);
+                        }
+                    }
+                    m[r] = mr;
+                }
             }
             a -= 1.0f;
             b -= 1.0f;
