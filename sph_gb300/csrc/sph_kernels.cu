@@ -677,7 +677,7 @@ __device__ __forceinline__ void density_one(int i, const Ctx &c, const float2 *_
     const float2 p = pos[i];
     const float2 mp = make_float2(-p.x, -p.y);
     const unsigned key = cell_key(p.x, p.y, g);
-    float a = 0.0f, b = 0.0f;
+    float2 ab = make_float2(0.0f, 0.0f);  // (rho, rho_near)
     unsigned long long m[3] = {0ull, 0ull, 0ull};
     int4 rec = make_int4(0, 0, 0, kRowsNone);
     if (searchable(key, i, start, g, capped, c.max_bucket)) {
@@ -701,14 +701,7 @@ __device__ __forceinline__ void density_one(int i, const Ctx &c, const float2 *_
                         const float r2 = dist2_packed(mp, __ldg(row + t), e);
                         if (r2 <= h2) {
                             mh[hh] |= 1u << (t & 31);
-                            const float rr = r2 > 0.0f ? r2 * rsqrtf(r2) : 0.0f;
-                            const float ratio = __fmul_rn(rr, h_recip);
-                            if (ratio < 1.0f) {
-                                const float omr = 1.0f - ratio;
-                                const float omr2 = omr * omr;
-                                a += omr2;
-                                b += omr2 * omr;
-                            }
+                            add_density(ab, r2, h_recip);
                         }
                     }
                 }
@@ -717,22 +710,13 @@ __device__ __forceinline__ void density_one(int i, const Ctx &c, const float2 *_
                 for (int t = kMaskRow; t < len; ++t) {
                     float2 e;
                     const float r2 = dist2_packed(mp, __ldg(row + t), e);
-                    if (r2 <= h2) {
-                        const float rr = r2 > 0.0f ? r2 * rsqrtf(r2) : 0.0f;
-                        const float ratio = __fmul_rn(rr, h_recip);
-                        if (ratio < 1.0f) {
-                            const float omr = 1.0f - ratio;
-                            const float omr2 = omr * omr;
-                            a += omr2;
-                            b += omr2 * omr;
-                        }
-                    }
+                    if (r2 <= h2) add_density(ab, r2, h_recip);
                 }
                 m[r] = ((unsigned long long)mh[1] << 32) | mh[0];
             }
             // the particle met itself (r = 0) in its own row: remove it
-            a -= 1.0f;
-            b -= 1.0f;
+            ab.x -= 1.0f;
+            ab.y -= 1.0f;
             const int self = i - ra[1];
             if (self < kMaskRow) m[1] &= ~(1ull << self);
         } else {
@@ -741,18 +725,11 @@ __device__ __forceinline__ void density_one(int i, const Ctx &c, const float2 *_
                 const float2 q = __ldg(pos + j);
                 const float r2 = dist2(p.x - q.x, p.y - q.y);
                 if (r2 > h2) return;
-                const float rr = r2 > 0.0f ? r2 * rsqrtf(r2) : 0.0f;
-                const float ratio = __fmul_rn(rr, h_recip);
-                if (ratio < 1.0f) {
-                    const float omr = 1.0f - ratio;
-                    const float omr2 = omr * omr;
-                    a += omr2;
-                    b += omr2 * omr;
-                }
+                add_density(ab, r2, h_recip);
             });
         }
     }
-    xr_out[i] = make_float4(p.x, p.y, a, b);
+    xr_out[i] = make_float4(p.x, p.y, ab.x, ab.y);
     mask01[i] = make_ulonglong2(m[0], m[1]);
     mask2[i] = m[2];
     if (rows_out) rows_out[i] = rec;

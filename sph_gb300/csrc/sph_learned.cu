@@ -104,7 +104,7 @@ k_features(Ctx c, const float2 *__restrict__ pos, const float2 *__restrict__ pre
     const float vix = (p.x - pp.x) * inv_dt, viy = (p.y - pp.y) * inv_dt;
     const float2 mp = make_float2(-p.x, -p.y);
     const unsigned key = cell_key(p.x, p.y, g);
-    float a = 0.0f, b = 0.0f;
+    float2 ab = make_float2(0.0f, 0.0f);  // (rho, rho_near), as density_one's
     unsigned long long m[3] = {0ull, 0ull, 0ull};
     float2 V1 = make_float2(0.0f, 0.0f), V2 = V1, Tdiag = V1, Dsum = V1;
     float Ms = 0.0f, Txy = 0.0f;
@@ -117,21 +117,19 @@ k_features(Ctx c, const float2 *__restrict__ pos, const float2 *__restrict__ pre
             int ra[3], rl[3];
             stencil_rows(key, start, g, ra, rl, c.n);
             // one neighbour's terms: density, messages, counts (self
-            // included in a and b, removed below)
+            // included in rho and rho_near, removed below)
             auto visit = [&](int j, const float2 &q) {
                 float2 e;  // q - p
                 const float r2 = dist2_packed(mp, q, e);
                 const float rinv = rsqrtf(r2);
-                const float rr = r2 > 0.0f ? r2 * rinv : 0.0f;
-                const float ratio = __fmul_rn(rr, h_recip);
+                const float ratio = __fmul_rn(sqrt_approx(r2), h_recip);
                 const bool other = j != i;
                 count += other ? 1 : 0;
                 degenerate |= other && r2 <= 2e-12f;
                 if (ratio < 1.0f) {
                     const float omr = 1.0f - ratio;
                     const float omr2 = omr * omr;
-                    a += omr2;
-                    b += omr2 * omr;
+                    ab = __ffma2_rn(make_float2(omr2, omr2), make_float2(1.0f, omr), ab);
                     if (other) {
                         // message sums in packed FP32x2 arithmetic
                         const float2 u = __fmul2_rn(e, make_float2(rinv, rinv));
@@ -188,8 +186,8 @@ k_features(Ctx c, const float2 *__restrict__ pos, const float2 *__restrict__ pre
                     m[r] = mr;
                 }
             }
-            a -= 1.0f;
-            b -= 1.0f;
+            ab.x -= 1.0f;
+            ab.y -= 1.0f;
             const int self = i - ra[1];
             if (self < kMaskRow) m[1] &= ~(1ull << self);
         } else {
@@ -199,17 +197,11 @@ k_features(Ctx c, const float2 *__restrict__ pos, const float2 *__restrict__ pre
                 const float2 q = __ldg(pos + j);
                 const float r2 = dist2(p.x - q.x, p.y - q.y);
                 if (r2 > h2) return;
-                const float rr = r2 > 0.0f ? r2 * rsqrtf(r2) : 0.0f;
-                const float ratio = __fmul_rn(rr, h_recip);
-                if (ratio < 1.0f) {
-                    const float omr = 1.0f - ratio;
-                    const float omr2 = omr * omr;
-                    a += omr2;
-                    b += omr2 * omr;
-                }
+                add_density(ab, r2, h_recip);
             });
         }
     }
+    const float a = ab.x, b = ab.y;
     xr_out[i] = make_float4(p.x, p.y, a, b);
     mask01[i] = make_ulonglong2(m[0], m[1]);
     mask2[i] = m[2];
