@@ -62,7 +62,9 @@ typedef struct sph_cuda_counters {
     unsigned int max_cell_occupancy;   /* largest cell population seen */
     unsigned int list_cap_risk;        /* nonzero if some half list could have exceeded
                                           max_neighbors (hash.c:188, 223); the cap is not
-                                          reproduced, see the design doc */
+                                          reproduced: the gathers search the full stencil,
+                                          so such a particle keeps neighbours the
+                                          reference would have dropped */
 } sph_cuda_counters;
 
 /* Creates a handle for up to max_particles particles.
@@ -231,7 +233,10 @@ int sph_cuda_rebuild_neighbors(sph_cuda_t *h);
 /* Waits for all queued work of the handle. */
 int sph_cuda_synchronize(sph_cuda_t *h);
 
-/* Copies the event counters out (synchronises). */
+/* Copies the event counters out (synchronises).  Returns SPH_ERR_CUDA (with
+ * the counters filled) if a step's cell build found its per-tile particle
+ * counts inconsistent with its cell counters -- an internal error after
+ * which the steps since the last upload are not valid. */
 int sph_cuda_get_counters(sph_cuda_t *h, sph_cuda_counters *out);
 
 /* FP64 diagnostics of the current state: out[0] mean density, out[1] mean

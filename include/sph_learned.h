@@ -1,7 +1,8 @@
 /*
  * sph_learned.h -- learned relaxation for libsph_cuda.  No counterpart in
  * the reference: it replaces most of the work of double_density_relaxation
- * (fluid.c:541-611), which stays as the fallback and the judge.
+ * (fluid.c:541-611), which stays as the fallback and the reference for
+ * training.
  *
  * Model.  A message-passing network over each particle's neighbours within h
  * (particles with more than 48 take the plain relaxation): messages are the
