@@ -524,6 +524,7 @@ __device__ __forceinline__ void viscosity_predict_one(
     const float h2 = __fmul_rn(hh, hh);
     const float h_recip = __fdiv_rn(1.0f, hh);
     const float sigma = __ldg(&S->P.sigma), beta = __ldg(&S->P.beta);
+    const float dt_h = dt * h_recip;
 
     const float2 p = pos[i];
     const float2 v0 = vel[i];  // before gravity: velocity differences need none
@@ -543,15 +544,16 @@ __device__ __forceinline__ void viscosity_predict_one(
         const float r_recip = rsqrtf(r2);
         const float r = r2 * r_recip;
         // gravity adds the same amount to both velocities: the difference
-        // is taken before it
-        const float u0 = ((v0.x - d.z) * qx + (v0.y - d.w) * qy) * r_recip;
+        // is taken before it (one packed subtraction)
+        const float2 w = __fadd2_rn(v0, make_float2(-d.z, -d.w));
+        const float u0 = (w.x * qx + w.y * qy) * r_recip;
         // only approaching pairs (u > 0) push; the others run the same
         // instructions with u = 0, whose impulse is +-0 and leaves dv's bits
         // as they are (no divergent branch: about half the pairs of every
         // warp approach)
         const float u = u0 > 0.0f ? u0 : 0.0f;
-        const float ratio = r * h_recip;
-        const float imp = dt * (1.0f - ratio) * (sigma * u + beta * u * u);
+        // dt (1 - r/h) (sigma u + beta u^2) = (dt - (dt/h) r) u (sigma + beta u)
+        const float imp = fmaf(-dt_h, r, dt) * u * fmaf(beta, u, sigma);
         // per component imp * q * r_recip, clamped, halved and subtracted
         // (packed FP32x2, each operation rounded as the scalar form)
         const float2 t = __fmul2_rn(__fmul2_rn(make_float2(imp, imp), e),
