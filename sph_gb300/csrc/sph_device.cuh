@@ -310,4 +310,31 @@ __device__ __forceinline__ void walk_mask(unsigned long long m, int base, int n,
     if (have) visit(jp, dp);
 }
 
+// The neighbours (r2 <= h2, r2 exact as dist2_packed rounds it) of one
+// stencil row of any length, in slot order: per chunk of 64 candidates a hit
+// mask from the position filter, then walk_mask over the hits.  For rows too
+// long for a stored mask; `self` (a slot or -1) is left out.
+template <class T, class Pos, class Load, class Visit>
+__device__ __forceinline__ void walk_row_hits(int a, int len, int self, int n, float2 mp, float h2,
+                                              Pos pos_of, Load load, Visit visit)
+{
+    for (int c0 = 0; c0 < len; c0 += 64) {
+        const int cl = min(len - c0, 64);
+        const int n0 = min(cl, 32);
+        unsigned lo = 0u, hi = 0u;
+        for (int t = 0; t < n0; ++t) {
+            float2 e;
+            lo |= (unsigned)(dist2_packed(mp, pos_of(a + c0 + t), e) <= h2) << t;
+        }
+        for (int t = 32; t < cl; ++t) {
+            float2 e;
+            hi |= (unsigned)(dist2_packed(mp, pos_of(a + c0 + t), e) <= h2) << (t - 32);
+        }
+        unsigned long long m = ((unsigned long long)hi << 32) | lo;
+        const int rel = self - (a + c0);
+        if (rel >= 0 && rel < 64) m &= ~(1ull << rel);
+        walk_mask<T>(m, a + c0, n, load, visit);
+    }
+}
+
 }  // namespace sph

@@ -853,7 +853,7 @@ struct LearnedIn {
     bool defer = false;  // leave the fallback particles to a second pass
 };
 
-template <bool PROBE, bool LEARNED = false>
+template <bool PROBE, bool LEARNED = false, bool LONG_ROWS = false>
 __device__ __forceinline__ void relax_update_one(
     int i, const Ctx &cx, const float4 *__restrict__ xr, const ulonglong2 *__restrict__ mask01,
     const unsigned long long *__restrict__ mask2, const int4 *__restrict__ rows,
@@ -918,7 +918,27 @@ __device__ __forceinline__ void relax_update_one(
         } else if (!capped) {
             int rl[3];
             stencil_rows(key, start, g, ra, rl, cx.n);
-            if (rl[0] <= kMaskRow && rl[1] <= kMaskRow && rl[2] <= kMaskRow) mode = kRowsMasked;
+            if (rl[0] <= kMaskRow && rl[1] <= kMaskRow && rl[2] <= kMaskRow) {
+                mode = kRowsMasked;
+            } else if (LONG_ROWS) {
+                // a row longer than one mask (dense cells): filter and walk
+                // 64 candidates at a time, in slot order -- for the fallback
+                // pass, whose particles are the dense ones (in the full pass
+                // the extra code costs the common path more than it saves)
+                const float2 mp = make_float2(-p.x, -p.y);
+                auto xr_pos = [&](int j) {
+                    const float4 q = __ldg(xr + j);
+                    return make_float2(q.x, q.y);
+                };
+                for (int r = 0; r < 3; ++r)
+                    walk_row_hits<float4>(
+                        ra[r], rl[r], r == 1 ? i : -1, cx.n, mp, c.h2, xr_pos,
+                        [&](int j) { return __ldg(xr + j); },
+                        [&](int j, const float4 &q) {
+                            relax_pair_walk(wc, p, q, i, j, S, ids, acc, nudges);
+                        });
+                mode = kRowsNone;
+            }
         }
     }
     if (mode == kRowsMasked) {
@@ -1047,8 +1067,9 @@ k_relax_fallback(Ctx c, const float4 *__restrict__ xr, const ulonglong2 *__restr
     if (t0 == 0) atomicAdd(&st->learned_fallback, (unsigned long long)total);
     const bool capped = *occ_in > (unsigned)c.max_bucket;
     for (unsigned k = t0; k < total; k += gridDim.x * blockDim.x)
-        relax_update_one<false>(fb_list[k], c, xr, mask01, mask2, rows, prev, ids, start, capped,
-                                pos_out, vel_out, kr_out, cnt, nullptr);
+        relax_update_one<false, false, true>(fb_list[k], c, xr, mask01, mask2, rows, prev, ids,
+                                             start, capped, pos_out, vel_out, kr_out, cnt,
+                                             nullptr);
 }
 
 // ---------------------------------------------------------------------------
