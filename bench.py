@@ -297,7 +297,7 @@ class DamBreak:
         sim.step(self.p(t))
 
     def tune(self, sim):
-        return sim.autotune(1)  # 48 steps with the tunables of the last step
+        return sim.autotune(3)  # 144 steps (3 interleaved rounds) with the last step's tunables
 
     def cpu_sample(self, args):
         return cpu_baseline_single(args.cpu_sample, args.cpu_steps)
@@ -327,7 +327,7 @@ class EnsembleWork:
         sim.step(None, 1)
 
     def tune(self, sim):
-        return sim.autotune(2)  # 96 steps (2 interleaved rounds)
+        return sim.autotune(3)  # 144 steps (3 interleaved rounds)
 
     def cpu_sample(self, args):
         import oracle
@@ -477,9 +477,10 @@ def run_skewed(args, world, rank):
 
     res = {}
     for label in ("plain", "learned"):
-        tuner = fresh(label == "learned")  # shapes tuned on a copy at step W
-        tuner.step(None, W)
-        shapes = tuner.autotune(1)
+        # shapes tuned on a copy at the middle of the timed window
+        tuner = fresh(label == "learned")
+        tuner.step(None, W + K // 2)
+        shapes = tuner.autotune(3)
         tuner.close()
         e = fresh(label == "learned")
         e.set_launch_shapes(shapes)
@@ -559,13 +560,14 @@ def run_gpu(args, world, rank):
     n, cells = work.n, work.cells
     K, W = args.steps, args.warmup
 
-    # ---- launch shapes: given, or tuned on a copy of the scene at step W, so
-    # that the timed steps are steps W .. W+K-1 of the run ----
+    # ---- launch shapes: given, or tuned on a copy of the scene advanced to
+    # the middle of the timed window (the gathers' costs drift as a scene
+    # compresses), so that the timed steps are steps W .. W+K-1 of the run ----
     if args.shapes:
         shapes = [int(v) for v in args.shapes.split(",")]
     else:
         tuner = work.fresh()
-        work.advance(tuner, 0, W)
+        work.advance(tuner, 0, W + K // 2)
         shapes = work.tune(tuner)
         tuner.close()
 

@@ -737,8 +737,10 @@ __device__ __forceinline__ void density_one(int i, const Ctx &c, const float2 *_
     if (rows_out) rows_out[i] = rec;
 }
 
+// 32 registers (four 512-thread CTAs' worth per SM): full occupancy for this
+// issue-bound pass outweighs the few spilled values of its rare paths.
 template <bool PERSIST>
-__global__ void __launch_bounds__(kMaxBlock)
+__global__ void __launch_bounds__(kMaxBlock, 4)
 k_density_t(Ctx c, const float2 *__restrict__ pos, const int *__restrict__ start,
             const unsigned *__restrict__ occ_in, float4 *__restrict__ xr_out,
             ulonglong2 *__restrict__ mask01, unsigned long long *__restrict__ mask2,
