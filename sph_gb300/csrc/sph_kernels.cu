@@ -631,8 +631,10 @@ __device__ __forceinline__ void viscosity_predict_one(
     kr_out[i] = make_uint2(k2, rank);
 }
 
+// 48 registers: more resident warps than the compiler's free choice (55),
+// without spills.
 template <bool PROBE, bool PERSIST = false>
-__global__ void __launch_bounds__(kMaxBlock)
+__global__ void __maxnreg__(48)
 k_viscosity_predict(Ctx c, const DevState *__restrict__ st, const float2 *__restrict__ pos,
                     const float2 *__restrict__ vel, const int *__restrict__ start,
                     const unsigned *__restrict__ occ_in, unsigned *occ_reset,
