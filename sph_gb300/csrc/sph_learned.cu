@@ -79,7 +79,9 @@ __device__ __forceinline__ float out_scale(const Scene *__restrict__ S)
 // coincident neighbour (r2 <= 2e-12, where the reference nudges) or in an
 // overflowing bucket gets count 65535: it always takes the plain
 // relaxation.  Block 0 resets the step's fallback-list counter.
-__global__ void __launch_bounds__(kBlock)
+// 40 registers: the occupancy this latency-bound gather gains is worth more
+// than the spills of its message sums (measured).
+__global__ void __maxnreg__(40)
 k_features(Ctx c, const float2 *__restrict__ pos, const float2 *__restrict__ prev,
            const int *__restrict__ start, const unsigned *__restrict__ occ_in,
            float4 *__restrict__ xr_out, ulonglong2 *__restrict__ mask01,
