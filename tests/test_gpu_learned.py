@@ -172,6 +172,29 @@ def test_fallback_only_is_the_plain_step(cuda_lib):
         assert learned.launches_per_step() == 11
 
 
+def test_fallback_only_is_the_plain_step_in_dense_cells(cuda_lib):
+    """Cells of 25 particles: stencil rows of ~75 candidates, longer than a
+    stored hit mask, so the plain relaxation searches the whole stencil and
+    the fallback pass walks the rows 64 candidates at a time -- the same
+    neighbours in the same order, bit for bit."""
+    sc = scenes.dam_break(6400, 80, 64.0, 64.0, seed=77, name="dense", lattice=0.2,
+                          x0=0.1, y0=0.1)
+    gx = np.floor(sc.x / sc.spacing).astype(np.int64)
+    gy = np.floor(sc.y / sc.spacing).astype(np.int64)
+    assert 3 * np.bincount(gy * sc.size_x + gx).max() > 64
+    P = sc.params.as_dict()
+    with Simulation.from_scene(sc) as plain, Simulation.from_scene(sc) as learned, \
+            LearnedModel(0, seed=5) as m:
+        plain.step(P, 2)
+        learned.step(P, 2)
+        learned.set_learned(m, threshold=-1.0)
+        plain.step(P, 4)
+        learned.step(P, 4)
+        a, b = plain.download(), learned.download()
+        for f in ("x", "y", "v_x", "v_y", "density", "density_near"):
+            assert bits_equal(a[f], b[f]), f
+
+
 def rms_density_error(sc, model, state_steps, threshold):
     """One step from the same state with and without the model: RMS of the
     density difference (by particle) in units of the rest density, and the
