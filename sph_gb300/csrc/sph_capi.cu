@@ -372,8 +372,24 @@ static int build_handle(sph_cuda **out, std::vector<Scene> &&scenes, int capacit
     return SPH_OK;
 }
 
-// Host SoA (x, y, vx, vy, x_prev, y_prev, rho, rho_near) -> device, then sort.
-// `fill(i, rec)` writes particle i's 8 floats.
+// The common tail of every upload: the particle count, a fresh device state,
+// zero tile counts and the sort into the A order (upload_soa_device).
+static int upload_finish(sph_cuda *h, int n)
+{
+    if (h->nscenes == 1 && h->scenes[0].n != n) {
+        h->scenes[0].n = n;
+        SPH_TRY(push_scenes(h));
+    }
+    h->n = n;
+    SPH_CUDA(cudaMemsetAsync(h->d_state, 0, sizeof(DevState), h->stream));
+    SPH_TRY(upload_soa_device(h, n));
+    SPH_CUDA(cudaStreamSynchronize(h->stream));  // the caller's buffers are free again
+    return SPH_OK;
+}
+
+// Host particles reached through a pointer array -> device, then sort.
+// `fill(i, rec)` writes particle i's 8 floats (x, y, vx, vy, x_prev, y_prev,
+// rho, rho_near) into a page-locked staging buffer, copied as four arrays.
 template <class Fill>
 static int upload_common(sph_cuda *h, int n, Fill fill)
 {
@@ -390,11 +406,6 @@ static int upload_common(sph_cuda *h, int n, Fill fill)
         prev[i] = make_float2(r[4], r[5]);
         xr[i] = make_float4(r[0], r[1], r[6], r[7]);
     }
-    if (h->nscenes == 1 && h->scenes[0].n != n) {
-        h->scenes[0].n = n;
-        SPH_TRY(push_scenes(h));
-    }
-    h->n = n;
     const size_t b = (size_t)n * sizeof(float2);
     if (n > 0) {
         SPH_CUDA(cudaMemcpyAsync(h->pos_b, pos, b, cudaMemcpyHostToDevice, h->stream));
@@ -402,10 +413,7 @@ static int upload_common(sph_cuda *h, int n, Fill fill)
         SPH_CUDA(cudaMemcpyAsync(h->prev_c, prev, b, cudaMemcpyHostToDevice, h->stream));
         SPH_CUDA(cudaMemcpyAsync(h->xr_c, xr, 2 * b, cudaMemcpyHostToDevice, h->stream));
     }
-    SPH_CUDA(cudaMemsetAsync(h->d_state, 0, sizeof(DevState), h->stream));
-    SPH_TRY(upload_soa_device(h, n));
-    SPH_CUDA(cudaStreamSynchronize(h->stream));  // staging buffer reuse
-    return SPH_OK;
+    return upload_finish(h, n);
 }
 
 // Sorted state -> id-order host SoA in the staging buffer (5 n float2:
@@ -580,6 +588,8 @@ int sph_cuda_upload(sph_cuda_t *h, fluid_particle *const *ptrs, int n)
     });
 }
 
+// The caller's contiguous arrays go to the device as they are (one copy
+// each, no host-side repacking) and a kernel lays them out.
 int sph_cuda_upload_particles(sph_cuda_t *h, const fluid_particle *ps, int n)
 {
     SPH_TRY(check_handle(h));
@@ -587,11 +597,16 @@ int sph_cuda_upload_particles(sph_cuda_t *h, const fluid_particle *ps, int n)
         set_error("null particle array");
         return SPH_ERR_INVALID;
     }
-    return upload_common(h, n, [&](int i, float *r) {
-        const fluid_particle *p = &ps[i];
-        r[0] = p->x; r[1] = p->y; r[2] = p->v_x; r[3] = p->v_y;
-        r[4] = p->x_prev; r[5] = p->y_prev; r[6] = p->density; r[7] = p->density_near;
-    });
+    SPH_TRY(check_n(h, n));
+    SPH_CUDA(cudaStreamSynchronize(h->stream));
+    if (n > 0) {
+        const size_t b = (size_t)n * sizeof(fluid_particle);
+        SPH_TRY(ensure_scratch(h, b));
+        auto *recs = static_cast<fluid_particle *>(h->d_scratch);
+        SPH_CUDA(cudaMemcpyAsync(recs, ps, b, cudaMemcpyHostToDevice, h->stream));
+        SPH_TRY(launch_upload_layout(h, n, nullptr, nullptr, nullptr, nullptr, recs));
+    }
+    return upload_finish(h, n);
 }
 
 int sph_cuda_upload_soa(sph_cuda_t *h, const float *x, const float *y, const float *vx,
@@ -602,10 +617,21 @@ int sph_cuda_upload_soa(sph_cuda_t *h, const float *x, const float *y, const flo
         set_error("x and y are required");
         return SPH_ERR_INVALID;
     }
-    return upload_common(h, n, [&](int i, float *r) {
-        r[0] = x[i]; r[1] = y[i]; r[2] = vx ? vx[i] : 0.0f; r[3] = vy ? vy[i] : 0.0f;
-        r[4] = x[i]; r[5] = y[i]; r[6] = 0.0f; r[7] = 0.0f;
-    });
+    SPH_TRY(check_n(h, n));
+    SPH_CUDA(cudaStreamSynchronize(h->stream));
+    if (n > 0) {
+        // the A-state arrays are free until the sort rewrites them
+        const size_t b = (size_t)n * sizeof(float);
+        float *dx = reinterpret_cast<float *>(h->pos_a), *dy = dx + n;
+        float *dvx = reinterpret_cast<float *>(h->vel_a), *dvy = dvx + n;
+        SPH_CUDA(cudaMemcpyAsync(dx, x, b, cudaMemcpyHostToDevice, h->stream));
+        SPH_CUDA(cudaMemcpyAsync(dy, y, b, cudaMemcpyHostToDevice, h->stream));
+        if (vx) SPH_CUDA(cudaMemcpyAsync(dvx, vx, b, cudaMemcpyHostToDevice, h->stream));
+        if (vy) SPH_CUDA(cudaMemcpyAsync(dvy, vy, b, cudaMemcpyHostToDevice, h->stream));
+        SPH_TRY(launch_upload_layout(h, n, dx, dy, vx ? dvx : nullptr, vy ? dvy : nullptr,
+                                     nullptr));
+    }
+    return upload_finish(h, n);
 }
 
 int sph_cuda_step(sph_cuda_t *h, const tunable_parameters *tp, int nsteps)

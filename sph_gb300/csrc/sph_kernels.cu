@@ -1468,6 +1468,53 @@ int step_kernel_count(const sph_cuda *h)
     return (h && h->learned) ? kLearnedStepKernels : kStepKernels;
 }
 
+// Host-layout particles, already on the device, -> the upload arrays in id
+// order: pos_b, vel_b, prev_c and xr_c = (x, y, rho, rho_near).  From
+// structure-of-arrays (vx, vy may be null: zero) or from the reference's
+// fluid_particle records.
+__global__ void __launch_bounds__(kBlock)
+k_upload_soa(int n, const float *__restrict__ x, const float *__restrict__ y,
+             const float *__restrict__ vx, const float *__restrict__ vy, float2 *__restrict__ pos,
+             float2 *__restrict__ vel, float2 *__restrict__ prev, float4 *__restrict__ xr)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float px = x[i], py = y[i];
+    pos[i] = make_float2(px, py);
+    vel[i] = make_float2(vx ? vx[i] : 0.0f, vy ? vy[i] : 0.0f);
+    prev[i] = make_float2(px, py);
+    xr[i] = make_float4(px, py, 0.0f, 0.0f);
+}
+
+__global__ void __launch_bounds__(kBlock)
+k_upload_records(int n, const fluid_particle *__restrict__ ps, float2 *__restrict__ pos,
+                 float2 *__restrict__ vel, float2 *__restrict__ prev, float4 *__restrict__ xr)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const fluid_particle &p = ps[i];
+    pos[i] = make_float2(p.x, p.y);
+    vel[i] = make_float2(p.v_x, p.v_y);
+    prev[i] = make_float2(p.x_prev, p.y_prev);
+    xr[i] = make_float4(p.x, p.y, p.density, p.density_near);
+}
+
+// Launches one of the two above on device copies of the caller's arrays
+// (x, y, vx, vy or recs; the others null).
+int launch_upload_layout(sph_cuda *h, int n, const float *x, const float *y, const float *vx,
+                         const float *vy, const fluid_particle *recs)
+{
+    if (n == 0) return SPH_OK;
+    const int nb = blocks_for(n);
+    if (recs)
+        k_upload_records<<<nb, kBlock, 0, h->stream>>>(n, recs, h->pos_b, h->vel_b, h->prev_c,
+                                                       h->xr_c);
+    else
+        k_upload_soa<<<nb, kBlock, 0, h->stream>>>(n, x, y, vx, vy, h->pos_b, h->vel_b, h->prev_c,
+                                                   h->xr_c);
+    return cuda_fail(cudaGetLastError(), "upload layout");
+}
+
 // Upload tail: pos_b / vel_b (id order) -> sorted A state; prev_c / xr_c
 // already hold the uploaded values in id order.
 int upload_soa_device(sph_cuda *h, int n)
