@@ -700,20 +700,29 @@ int sph_cuda_download_particles(sph_cuda_t *h, fluid_particle *ps, int n)
     return SPH_OK;
 }
 
+// Laid out on the device and copied straight into the caller's arrays (no
+// host-side repacking).
 int sph_cuda_download_soa(sph_cuda_t *h, float *x, float *y, float *vx, float *vy, float *rho,
                           float *rho_near, int n)
 {
     SPH_TRY(check_handle(h));
-    float2 *s = nullptr;
-    SPH_TRY(download_common(h, n, &s));
-    for (int i = 0; i < n; ++i) {
-        if (x) x[i] = s[i].x;
-        if (y) y[i] = s[i].y;
-        if (vx) vx[i] = s[n + i].x;
-        if (vy) vy[i] = s[n + i].y;
-        if (rho) rho[i] = s[3 * n + i].x;
-        if (rho_near) rho_near[i] = s[3 * n + i].y;
+    if (n != h->n) {
+        set_error("download of %d particles, handle holds %d", n, h->n);
+        return SPH_ERR_INVALID;
     }
+    if (n == 0) return SPH_OK;
+    const size_t rec = (size_t)n * 5 * sizeof(float2), col = (size_t)n * sizeof(float);
+    SPH_TRY(ensure_scratch(h, rec + 6 * col + 16));
+    float2 *s = static_cast<float2 *>(h->d_scratch);
+    float *cols = reinterpret_cast<float *>(s + 5 * (size_t)n);
+    SPH_TRY(launch_unpermute(h, s));
+    SPH_TRY(launch_split_soa(h, n, s, cols));
+    float *dst[6] = {x, y, vx, vy, rho, rho_near};
+    for (int k = 0; k < 6; ++k)
+        if (dst[k])
+            SPH_CUDA(cudaMemcpyAsync(dst[k], cols + k * (size_t)n, col, cudaMemcpyDeviceToHost,
+                                     h->stream));
+    SPH_CUDA(cudaStreamSynchronize(h->stream));
     return SPH_OK;
 }
 

@@ -196,6 +196,7 @@ int ensure_stage(sph_cuda *h, size_t bytes);
 int upload_soa_device(sph_cuda *h, int n);  // pos_b/vel_b (id order) + xr_c -> state
 int launch_upload_layout(sph_cuda *h, int n, const float *x, const float *y, const float *vx,
                          const float *vy, const fluid_particle *recs);
+int launch_split_soa(sph_cuda *h, int n, const float2 *rec, float *out);
 int set_scene_params(sph_cuda *h, int scene, const tunable_parameters *tp);
 int enqueue_step(sph_cuda *h, cudaEvent_t *events, int *nkernels);
 unsigned bounds_flags_kernels();  // checked builds (SPH_BOUNDS_CHECK): recorded index faults

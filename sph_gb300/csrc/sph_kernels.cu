@@ -1515,6 +1515,31 @@ int launch_upload_layout(sph_cuda *h, int n, const float *x, const float *y, con
     return cuda_fail(cudaGetLastError(), "upload layout");
 }
 
+// The id-order records of k_unpermute (pos, vel, prev, (rho, rho_near),
+// pressures; n float2 each) -> six float arrays x, y, vx, vy, rho, rho_near
+// (n each, in that order), for copies straight into the caller's arrays.
+__global__ void __launch_bounds__(kBlock)
+k_split_soa(int n, const float2 *__restrict__ rec, float *__restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const size_t m = (size_t)n;
+    const float2 p = rec[i], v = rec[m + i], r = rec[3 * m + i];
+    out[i] = p.x;
+    out[m + i] = p.y;
+    out[2 * m + i] = v.x;
+    out[3 * m + i] = v.y;
+    out[4 * m + i] = r.x;
+    out[5 * m + i] = r.y;
+}
+
+int launch_split_soa(sph_cuda *h, int n, const float2 *rec, float *out)
+{
+    if (n == 0) return SPH_OK;
+    k_split_soa<<<blocks_for(n), kBlock, 0, h->stream>>>(n, rec, out);
+    return cuda_fail(cudaGetLastError(), "split");
+}
+
 // Upload tail: pos_b / vel_b (id order) -> sorted A state; prev_c / xr_c
 // already hold the uploaded values in id order.
 int upload_soa_device(sph_cuda *h, int n)
