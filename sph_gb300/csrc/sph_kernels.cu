@@ -485,6 +485,91 @@ k_permute(int n, const uint2 *__restrict__ kr, const int *__restrict__ start,
     if (b_src) b_dst[d] = b_src[i];
 }
 
+// The step's forms of k_scatter_ids and k_permute: K particles per thread
+// (strided by the block size, so the loads stay coalesced), their loads
+// issued together, so that each thread has K dependent chains (key -> cell
+// start -> slot) in flight instead of one.
+template <int K>
+__global__ void __launch_bounds__(kBlock)
+k_scatter_ids_x(int n, const uint2 *__restrict__ kr, const int *__restrict__ id_src,
+                const int *__restrict__ start, int *__restrict__ tmp, unsigned *tile_cnt,
+                int ntiles)
+{
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    for (int t = g; t < ntiles; t += gridDim.x * blockDim.x) tile_cnt[t] = 0u;
+    const int i0 = blockIdx.x * blockDim.x * K + threadIdx.x;
+    uint2 k[K];
+    int id[K], st[K];
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+        const int i = i0 + j * blockDim.x;
+        if (i < n) {
+            k[j] = kr[i];
+            id[j] = id_src ? id_src[i] : i;
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < K; ++j)
+        if (i0 + j * (int)blockDim.x < n) st[j] = __ldg(start + k[j].x);
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+        if (i0 + j * (int)blockDim.x >= n) continue;
+        const int d = st[j] + (int)k[j].y;
+        if (in_bounds(d, n, kBadScatter)) tmp[d] = id[j];
+    }
+}
+
+template <int K>
+__global__ void __launch_bounds__(kBlock)
+k_permute_x(int n, const uint2 *__restrict__ kr, const int *__restrict__ start,
+            const int *__restrict__ tmp, const int *__restrict__ id_src,
+            const float2 *__restrict__ a_src, const float2 *__restrict__ b_src,
+            int *__restrict__ id_dst, float2 *__restrict__ a_dst, float2 *__restrict__ b_dst,
+            DevState *__restrict__ end_step)
+{
+    if (end_step && blockIdx.x == 0 && threadIdx.x == 0) {
+        end_step->lists_valid = 1u;
+        end_step->steps += 1ull;
+    }
+    const int i0 = blockIdx.x * blockDim.x * K + threadIdx.x;
+    uint2 k[K];
+    int id[K], s0[K], s1[K];
+    float2 a[K], b[K];
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+        const int i = i0 + j * blockDim.x;
+        if (i < n) {
+            k[j] = kr[i];
+            id[j] = id_src ? id_src[i] : i;
+            a[j] = a_src[i];
+            if (b_src) b[j] = b_src[i];
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < K; ++j)
+        if (i0 + j * (int)blockDim.x < n) {
+            s0[j] = __ldg(start + k[j].x);
+            s1[j] = __ldg(start + k[j].x + 1);
+        }
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+        if (i0 + j * (int)blockDim.x >= n) continue;
+        int r;
+        if (s1[j] - s0[j] <= kRankScanMax) {
+            r = 0;
+            for (int q = s0[j]; q < s1[j]; ++q)
+                if (in_bounds(q, n, kBadScatter)) r += __ldg(tmp + q) < id[j];
+        } else {
+            r = (int)k[j].y;  // pathological cell: arrival order
+        }
+        const int d = s0[j] + r;
+        if (!in_bounds(d, n, kBadScatter)) continue;
+        id_dst[d] = id[j];
+        a_dst[d] = a[j];
+        if (b_src) b_dst[d] = b[j];
+    }
+}
+
 // Cell keys of uploaded positions (id order, no step before them).
 __global__ void __launch_bounds__(kBlock)
 k_keys(Ctx c, const float2 *__restrict__ pos, uint2 *__restrict__ kr, unsigned *__restrict__ cnt,
@@ -1304,6 +1389,8 @@ static int launch_scan(sph_cuda *h, unsigned *in, int M, int *out, unsigned *occ
 // `out` (M + 1 entries); the build's key producer counted its particles per
 // build tile into build_tiles, which the build's scatter zeroes again.
 static int build_tiles_of(const sph_cuda *h) { return (h->M + kBuildTile - 1) / kBuildTile; }
+// particles per thread of the step's scatter and permute
+constexpr int kBuildPerThread = 2;
 
 static void enqueue_cell_starts(sph_cuda *h, int *out, unsigned *occ)
 {
@@ -1342,11 +1429,13 @@ static void enqueue_predict_sort(sph_cuda *h, Mark &mark)
     mark();
     enqueue_cell_starts(h, h->start_c, &st->build_max_occ[SLOT_PREDICTED]);
     mark();
-    k_scatter_ids<<<nb, kBlock, 0, h->stream>>>(n, h->kr_b, h->id_a, h->start_c, h->tmp_id,
-                                                h->build_tiles, build_tiles_of(h));
+    const int nbx = blocks_for(n, kBlock * kBuildPerThread);
+    k_scatter_ids_x<kBuildPerThread><<<nbx, kBlock, 0, h->stream>>>(
+        n, h->kr_b, h->id_a, h->start_c, h->tmp_id, h->build_tiles, build_tiles_of(h));
     mark();
-    k_permute<<<nb, kBlock, 0, h->stream>>>(n, h->kr_b, h->start_c, h->tmp_id, h->id_a, h->pos_b,
-                                            h->prev_b, h->id_c, h->pos_c, h->prev_c, nullptr);
+    k_permute_x<kBuildPerThread><<<nbx, kBlock, 0, h->stream>>>(
+        n, h->kr_b, h->start_c, h->tmp_id, h->id_a, h->pos_b, h->prev_b, h->id_c, h->pos_c,
+        h->prev_c, nullptr);
     mark();
 }
 
@@ -1441,11 +1530,13 @@ int enqueue_step(sph_cuda *h, cudaEvent_t *events, int *nkernels)
     }
     enqueue_cell_starts(h, h->start_a, &st->build_max_occ[SLOT_RELAXED]);
     mark();
-    k_scatter_ids<<<nb, kBlock, 0, h->stream>>>(n, h->kr_b, h->id_c, h->start_a, h->tmp_id,
-                                                h->build_tiles, build_tiles_of(h));
+    const int nbx = blocks_for(n, kBlock * kBuildPerThread);
+    k_scatter_ids_x<kBuildPerThread><<<nbx, kBlock, 0, h->stream>>>(
+        n, h->kr_b, h->id_c, h->start_a, h->tmp_id, h->build_tiles, build_tiles_of(h));
     mark();
-    k_permute<<<nb, kBlock, 0, h->stream>>>(n, h->kr_b, h->start_a, h->tmp_id, h->id_c, h->pos_b,
-                                            h->vel_b, h->id_a, h->pos_a, h->vel_a, st);
+    k_permute_x<kBuildPerThread><<<nbx, kBlock, 0, h->stream>>>(
+        n, h->kr_b, h->start_a, h->tmp_id, h->id_c, h->pos_b, h->vel_b, h->id_a, h->pos_a,
+        h->vel_a, st);
     mark();
     if (nkernels) *nkernels = e - 1;
     return cuda_fail(cudaGetLastError(), "step launch");
