@@ -43,3 +43,23 @@ def test_traffic_capture_covers_the_step_kernels(cuda_lib):
 def test_canonical_step_bytes():
     sc = scenes.config2()
     assert scenes.algorithmic_bytes_per_step(sc.n, sc.cells) == 216 * 4_194_304 + 16 * 6_444_050 == 1_009_074_464
+
+
+def test_reference_arm_prints_the_contract_line(tmp_path):
+    """`bench.py --impl reference` on a tiny sample: one JSON line with the
+    reference arm's keys (it runs the CPU step only, no GPU)."""
+    import subprocess
+    import sys
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
+                          "--cpu-sample", "4096", "--cpu-steps", "2"],
+                         capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [l for l in out.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["metric"] == "particle-steps/s" and d["value"] > 0
+    assert d["higher_is_better"] is True and d["unit"] == "particle-steps/s"
+    assert d["cpu_baseline"]["value"] == d["value"] and d["cpu_baseline"]["cores"] >= 1
+    assert d["cpu_baseline"]["kind"] in ("port", "reference")
+    assert d["e2e"] == {"value": d["value"], "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}
