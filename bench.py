@@ -183,30 +183,6 @@ def max_over_ranks(world, v: float) -> float:
     return float(t.item())
 
 
-def cpu_sample_scene(n_sample: int):
-    from sph_gb300 import scenes
-    return scenes.config2(n=n_sample)
-
-
-def time_cpu_port(n_sample: int, steps: int, kind: str):
-    """Seconds for `steps` reference steps (Gauss-Seidel order) of a sample."""
-    import oracle
-    sc = cpu_sample_scene(n_sample)
-    sim = oracle.Sim(kind, sc.x, sc.y, sc.vx, sc.vy, sc.params.as_dict(), sc.config())
-    mv = sc.mover_schedule(0, steps + 1)
-    sim.step(1, mv[:1])  # first step (no viscosity) outside the timing
-    t0 = time.perf_counter()
-    sim.step(steps, mv[1:])
-    dt = time.perf_counter() - t0
-    sim.close()
-    return dt
-
-
-def _cpu_worker(args):
-    n_sample, steps, kind = args
-    return time_cpu_port(n_sample, steps, kind)
-
-
 def cpu_kind():
     import oracle
     if not os.path.exists(oracle.PORT_LIB):
@@ -214,46 +190,86 @@ def cpu_kind():
     return ("ref", "reference") if oracle.ref_available() else ("port", "port")
 
 
-def cpu_baseline_single(n_sample=262_144, steps=12):
+def time_cpu_slab(n: int, slab: int, nslabs: int, warmup: int, steps: int, kind: str):
+    """One compute rank of the reference's decomposition of the dam break:
+    x-slab `slab` of `nslabs` (geometry.c:101-160), its particles stepped by
+    the reference's single-rank step loop (fluid.c:273-348) in the global
+    box and grid, with the global mover schedule.  `warmup` untimed steps
+    (the first has no viscosity, fluid.c:202), then `steps` timed ones.
+    Returns (particles, seconds)."""
+    import oracle
+    from sph_gb300 import scenes
+    sc = scenes.config2(n=n)
+    idx = scenes.slab_indices(sc, slab, nslabs)
+    sim = oracle.Sim(kind, sc.x[idx], sc.y[idx], sc.vx[idx], sc.vy[idx], sc.params.as_dict(),
+                     sc.config())
+    mv = sc.mover_schedule(0, warmup + steps)
+    sim.step(warmup, mv[:warmup])
+    t0 = time.perf_counter()
+    sim.step(steps, mv[warmup:])
+    dt = time.perf_counter() - t0
+    sim.close()
+    return len(idx), dt
+
+
+def _slab_worker(args):
+    return time_cpu_slab(*args)
+
+
+def cpu_baseline_single(n, cores_hint, steps=12):
+    """The reference step on one host core: the middle x-slab (the one the
+    mover stirs) of the dam break cut into as many slabs as the host has
+    cores, 12 steps after one untimed step."""
     kind, label = cpu_kind()
-    dt = time_cpu_port(n_sample, steps, kind)
-    return {"value": n_sample * steps / dt, "unit": "particle-steps/s", "cores": 1, "kind": label,
-            "sample": f"dam break construction of the 4M workload scaled to {n_sample} particles "
-                      f"(same lattice, fill fraction, moving sphere mover), {steps} steps after one "
-                      f"untimed step, reference step order, single thread, -O2 -ffp-contract=off"}
+    nslabs = max(1, cores_hint)
+    slab = nslabs // 2
+    m, dt = time_cpu_slab(n, slab, nslabs, 1, steps, kind)
+    return {"value": m * steps / dt, "unit": "particle-steps/s", "cores": 1, "kind": label,
+            "sample": f"x-slab {slab} of the {n}-particle dam break cut into {nslabs} slabs as "
+                      f"partitionProblem cuts it (geometry.c:101-160): {m} particles, {steps} steps "
+                      f"after one untimed step, reference step order (Gauss-Seidel), single thread, "
+                      f"-O2 -ffp-contract=off; no halo exchange"}
 
 
 def run_reference(args, world, rank):
-    """The reference's CPU step on all host cores: one independent process
-    per core, each the single-rank step loop on a sample of the workload."""
+    """The reference's CPU step on all host cores, on the same dam break:
+    the scene is cut into one x-slab per core exactly as partitionProblem
+    (geometry.c:101-160) assigns particle columns to compute ranks, and each
+    core runs its slab's single-rank step loop (fluid.c:273-348) for W
+    untimed and K timed steps.  MPI is absent on the host, so the slabs do
+    not exchange halos or migrants (communication.c): each slab is stepped as
+    its own domain in the global box, an upper bound of the reference's
+    multi-rank throughput.  value = all slabs' particles x K / the slowest
+    slab's time."""
     if rank != 0:
         return
     import multiprocessing as mp
     kind, label = cpu_kind()
     cores = os.cpu_count() or 1
-    n_sample, steps = args.cpu_sample, max(2, args.cpu_steps)
+    K, W = args.steps, args.warmup
     ctx = mp.get_context("spawn")
-    work = [(n_sample, steps, kind)] * cores
-    for _ in range(max(0, min(args.warmup, 1))):
-        pass
+    work = [(args.n, s, cores, W, K, kind) for s in range(cores)]
     t0 = time.perf_counter()
     with ctx.Pool(cores) as pool:
-        times = pool.map(_cpu_worker, work)
+        res = pool.map(_slab_worker, work)
     wall = time.perf_counter() - t0
-    busy = max(times)
-    value = cores * n_sample * steps / busy
+    total = sum(m for m, _ in res)
+    busy = max(dt for _, dt in res)
+    value = total * K / busy
+    sizes = [m for m, _ in res]
     line = {"metric": "particle-steps/s", "value": value, "unit": "particle-steps/s",
-            "impl": "reference", "n_gpus": args.gpus, "steps": steps, "warmup": 1,
-            "ms_per_step": 1e3 * busy / steps, "higher_is_better": True, "scaling": "weak",
+            "impl": "reference", "n_gpus": args.gpus, "steps": K, "warmup": W,
+            "ms_per_step": 1e3 * busy / K, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "dam break, 4,194,304-particle construction sampled at "
-                                   f"{n_sample} particles per core", "particles_per_core": n_sample,
-                       "cores": cores, "wall_s": wall},
+            "config": {"workload": f"dam break, {total} particles, box 3,590h x 1,795h, moving sphere "
+                                   f"mover r=8h, plain method (reference step order)",
+                       "particles": total, "slabs": cores, "slab_particles": [min(sizes), max(sizes)],
+                       "steps_timed": f"{W}..{W + K - 1}", "wall_s": wall},
             "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": cores, "kind": label,
-                             "sample": f"{cores} independent processes, each the reference's single-rank "
-                                       f"step loop (Gauss-Seidel order, fluid.c:273-348) on a {n_sample}-"
-                                       f"particle sample of the dam break for {steps} steps; no halo "
-                                       f"exchange, so an upper bound of {cores}-rank MPI throughput"},
+                             "sample": f"the whole workload: {cores} x-slabs cut as partitionProblem cuts "
+                                       f"them (geometry.c:101-160), one per core, each the reference's "
+                                       f"single-rank step loop (fluid.c:273-348), steps {W}..{W + K - 1}; "
+                                       f"no halo exchange or migration between slabs (no MPI on the host)"},
             "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -300,7 +316,7 @@ class DamBreak:
         return sim.autotune(3)  # 144 steps (3 interleaved rounds) with the last step's tunables
 
     def cpu_sample(self, args):
-        return cpu_baseline_single(args.cpu_sample, args.cpu_steps)
+        return cpu_baseline_single(self.n, os.cpu_count() or 1, args.cpu_steps)
 
 
 class EnsembleWork:
@@ -550,6 +566,80 @@ def run_skewed(args, world, rank):
         print(json.dumps(line), flush=True)
 
 
+def _gather_lists(counts, ids, owners):
+    """Concatenated half lists of `owners` (ids into counts/ids as
+    neighbor_lists returns them: counts by id, lists in id order)."""
+    import numpy as np
+    off = np.zeros(len(counts) + 1, np.int64)
+    np.cumsum(counts, out=off[1:])
+    lens = counts[owners].astype(np.int64)
+    total = int(lens.sum())
+    if total == 0:
+        return np.zeros(0, ids.dtype)
+    first = np.repeat(off[owners] - np.concatenate([[0], np.cumsum(lens)[:-1]]), lens)
+    return ids[first + np.arange(total)]
+
+
+def parity_window(sim, sc, params, cx0=560, cx1=640):
+    """Parity of a full-size state against the oracle, on a window of it.
+    The particles of grid columns [cx0, cx1) (the full height: the dense
+    floor, the free surface, and the mover's path) are given, in id order,
+    to the pinned CPU restatement of hash_fluid (hash.c:127-242) on the same
+    grid; for the particles of columns [cx0 + 1, cx1 - 1), whose whole 3x3
+    stencil lies in the window, the library's half lists over the WHOLE
+    state must equal the oracle's (bit for bit, in the reference's order),
+    their densities the reference's FP32 densities within 1e-5 relative per
+    particle, and their relaxation displacements the FP64 gather oracle
+    (fluid.c:541-611, from the library's densities) within 1e-5 of the
+    summed magnitude of their pair terms."""
+    import numpy as np
+
+    import oracle
+    t0 = time.perf_counter()
+    st = sim.download()
+    counts, ids = sim.neighbor_lists()
+    rho, rhon = sim.probe_density(params)
+    dx, dy = sim.probe_relaxation(params)
+    x, y = st["x"], st["y"]
+    with np.errstate(invalid="ignore"):
+        cx = np.floor(x / np.float32(sc.spacing))
+    win = np.nonzero((cx >= cx0) & (cx < cx1) & np.isfinite(y) & (y >= 0))[0]
+    inner = (cx[win] >= cx0 + 1) & (cx[win] < cx1 - 1)
+    z = np.zeros(len(win), np.float32)
+    orc = oracle.Sim("port", x[win], y[win], z, z, params, sc.config())
+    oc, oi = orc.hash(compute_density=True)
+    ost = orc.get()
+    loc = np.nonzero(inner)[0]
+    g_own = win[loc]
+    lists_ok = bool(np.array_equal(counts[g_own], oc[loc]) and
+                    np.array_equal(_gather_lists(counts, ids, g_own),
+                                   win[_gather_lists(oc, oi, loc)]))
+    dens_err = 0.0
+    dens_ok = True
+    for got, want in ((rho[g_own], ost["density"][loc]), (rhon[g_own], ost["density_near"][loc])):
+        got, want = got.astype(np.float64), want.astype(np.float64)
+        d = np.abs(got - want)
+        nz = want != 0
+        dens_ok &= bool(np.all(d[~nz] == 0))
+        dens_err = max(dens_err, float(np.max(d[nz] / np.abs(want[nz]), initial=0.0)))
+    ox, oy, scale = orc.relax_f64(rho[win], rhon[win])
+    orc.close()
+    rel = 0.0
+    relax_ok = True
+    for got, want in ((dx[g_own], ox[loc]), (dy[g_own], oy[loc])):
+        err = np.abs(got.astype(np.float64) - want)
+        relax_ok &= bool(np.all(err <= 1e-5 * scale[loc] + 1e-9))
+        rel = max(rel, float(np.max(err / (scale[loc] + 1e-30), initial=0.0)))
+    return {"lists_bit_exact": lists_ok, "density_max_rel": dens_err,
+            "density_ok": dens_ok and dens_err <= 1e-5,
+            "relax_max_rel": rel, "relax_ok": relax_ok,
+            "relax_tolerance": "|err| <= 1e-5 * sum |pair terms| + 1e-9 per component",
+            "particles_checked": int(len(loc)), "window_particles": int(len(win)),
+            "window": f"grid columns [{cx0 + 1}, {cx1 - 1}) of {sc.size_x}, full height",
+            "half_list_entries_checked": int(counts[g_own].sum()),
+            "seconds": time.perf_counter() - t0}
+
+
 def run_gpu(args, world, rank):
     import numpy as np
 
@@ -593,6 +683,29 @@ def run_gpu(args, world, rank):
     # ---- per-kernel times (CUDA events on the library stream) ----
     kt_runs = [sim.kernel_times(None) for _ in range(5)]
     ktimes = {k: statistics.median(r[k] for r in kt_runs) for k in kt_runs[0]}
+    t_now = t0 + K + len(kt_runs)
+
+    # ---- parity of this full-size state against the oracle (config 2) ----
+    parity = None
+    if args.workload == "dam_break" and not args.no_parity and rank == 0:
+        try:
+            parity = parity_window(sim, work.sc, work.p(t_now))
+        except Exception as exc:  # reported, never hidden
+            parity = {"error": f"{type(exc).__name__}: {exc}"}
+
+    # ---- the same scene later in the run (compressed fluid) ----
+    late = None
+    if args.workload == "dam_break" and args.late_start > t_now and args.late_steps > 0:
+        work.advance(sim, t_now, args.late_start - t_now)
+        sim.synchronize()
+        sim.timer_start()
+        work.advance(sim, args.late_start, args.late_steps)
+        ms_late = sim.timer_stop()
+        late = {"steps_timed": f"{args.late_start}..{args.late_start + args.late_steps - 1}",
+                "ms_per_step": ms_late / args.late_steps,
+                "value": n * args.late_steps / (ms_late / 1e3),
+                "step_frac": scenes.algorithmic_bytes_per_step(n, cells)
+                / (ms_late / args.late_steps / 1e3) / 1e9 / load_peaks()[0]}
     sim.close()
     top = max(ktimes, key=ktimes.get)
     per_p, per_c = ALG_BYTES[top]
@@ -655,6 +768,7 @@ def run_gpu(args, world, rank):
                            "l2": "no flush: per-step working set ~0.5 GB > 129 MB L2",
                            "steps_timed": f"{t0}..{t0 + K - 1}", "launch_shapes": shapes},
                 "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
+                "parity": parity, "late_window": late,
                 "clocks": clocks, "gpu_launches": launches, "learned": learned,
                 "diagnostics": {"mean_density": diag[0], "mean_near_density": diag[1],
                                 "kinetic_energy_per_particle": diag[2]},
@@ -673,13 +787,16 @@ def main():
     ap.add_argument("--scenes", type=int, default=512)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--cpu-sample", type=int, default=262_144)
     ap.add_argument("--cpu-steps", type=int, default=12)
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--shapes", default="",
                     help="six ints: the gathers' launch shapes, instead of autotuning "
                          "(profiling runs: under a profiler the tuner's timings are not real)")
     ap.add_argument("--no-trajectory", action="store_true")
+    ap.add_argument("--no-parity", action="store_true")
+    ap.add_argument("--late-start", type=int, default=480,
+                    help="a second timed window of --late-steps steps from this step of the run")
+    ap.add_argument("--late-steps", type=int, default=20)
     ap.add_argument("--learned-threshold", type=float, default=0.01)
     ap.add_argument("--train-scenes", type=int, default=200)
     ap.add_argument("--train-n", type=int, default=65_536)

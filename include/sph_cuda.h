@@ -10,8 +10,8 @@
  *
  * Replaces, for a single-device domain, the compute rank's loop body
  * fluid.c:273-348 (with the MPI halo/migration calls of fluid.c:310-349
- * gone: one domain, no neighbours).  The caller-side switch is shown in
- * INTEGRATION.md.
+ * gone: one domain, no neighbours): the caller creates a handle and uploads
+ * its particles once, then calls sph_cuda_step where the loop body was.
  *
  * Conventions
  *  - Every call returns an sph_status (0 = SPH_OK).  On failure
@@ -290,14 +290,27 @@ int sph_cuda_probe_viscosity(sph_cuda_t *h, const tunable_parameters *tp, float 
  * array inside the library (about 7 MB, held on every GPU that loads the
  * library until the process exits).  Rejects n > SPH_STATIC_MAX_PARTICLES
  * and size_x * size_y > SPH_STATIC_MAX_CELLS with SPH_ERR_CAPACITY.
- * The first call on a device looks up that array's device address; make
- * that first call before any stream capture.  Work is queued on `stream`
+ * Each call outside stream capture looks up that array's device address (a
+ * call under capture reuses the last one found on the device), so make the
+ * first call on a device before any stream capture.  Work is queued on `stream`
  * (NULL = the default stream) and the call returns once it is queued.
  * All calls share the one array: calls whose work overlaps on the GPU (other
  * streams, other host threads) race and corrupt each other's results. */
 int sph_cuda_density_static(const float *x, const float *y, int n, const neighbor_grid_t *grid,
                             const tunable_parameters *tp, float *density, float *density_near,
                             void *stream);
+
+/* The event counters of the last sph_cuda_density_static call's neighbour
+ * build, written to caller-owned DEVICE memory *d_out on `stream` (steps is
+ * 0): out_of_grid counts particles whose cell key fell outside the grid
+ * (they get zero density), bucket_overflow the particles dropped beyond
+ * max_bucket_size in their cell, max_cell_occupancy the fullest cell, and
+ * list_cap_risk is nonzero when a cell held enough particles for a half
+ * list to pass max_neighbors (the density pass does not cut lists, so such
+ * a particle keeps neighbours the reference would have dropped).  Allocates
+ * nothing; queue it after the density call on the same stream, before any
+ * other call reuses the shared array. */
+int sph_cuda_density_static_counters(sph_cuda_counters *d_out, void *stream);
 
 /* ---- measurement ---- */
 

@@ -26,7 +26,11 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_LIB = os.path.join(HERE, "libsph_oracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libsph_ref.so")
 REF_FASTMATH_LIB = os.path.join(HERE, "_ref", "libsph_ref_fastmath.so")
-REF_SRC = "/root/reference/src"
+# Where the reference's src/ lies: $SPH_REF_SRC, else a checkout named
+# "reference" beside this repository.  Absent (as on a machine that only
+# runs the GPU tests), the "ref" back end is simply not built.
+REF_SRC = os.environ.get("SPH_REF_SRC") or os.path.join(
+    os.path.dirname(os.path.dirname(HERE)), "reference", "src")
 
 FIELDS = ("x_prev", "y_prev", "x", "y", "v_x", "v_y", "a_x", "a_y", "density",
           "density_near", "pressure", "pressure_near")

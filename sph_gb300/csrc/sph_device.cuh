@@ -136,25 +136,22 @@ __device__ __forceinline__ float dist2(float dx, float dy)
 // component (given mp = -p), r2 = d.x^2 + d.y^2, each operation rounded
 // exactly as dist2(p.x - q.x, p.y - q.y) rounds it (the squares of +-dx
 // are equal), in three instructions instead of five.
-// Square root by PTX sqrt.approx.f32 (one special-function op; 0 gives 0):
-// the distances of the density sums, which need no correctly rounded root.
-__device__ __forceinline__ float sqrt_approx(float x)
-{
-    float y;
-    asm("sqrt.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
-}
-
 // One neighbour's share of (rho, rho_near): ((1 - r/h)^2, (1 - r/h)^3) for
-// r/h < 1 (calculate_density, fluid.c:527-539), added to ab with one packed
-// FMA (rho + omr2 * 1 rounds as rho + omr2).
+// r/h < 1 (calculate_density, fluid.c:527-539), each term rounded exactly as
+// the reference rounds it: r = sqrt(r2) correctly rounded (hash.c:190 takes
+// the double root of the float r2 and stores it as a float, which is the
+// correctly rounded float root), ratio = r * (1/h) (hash.c:191), w = 1 -
+// ratio, then w*w and (w*w)*w.  Near r = h the subtraction w = 1 - ratio
+// cancels, so a root that is off by one unit would change a sparse
+// particle's density by far more than 1e-5; with the same terms, only the
+// order of the (positive) sum differs from the reference.
 __device__ __forceinline__ void add_density(float2 &ab, float r2, float h_recip)
 {
-    const float ratio = __fmul_rn(sqrt_approx(r2), h_recip);
+    const float ratio = __fmul_rn(__fsqrt_rn(r2), h_recip);
     if (ratio < 1.0f) {
-        const float omr = 1.0f - ratio;
-        const float omr2 = omr * omr;
-        ab = __ffma2_rn(make_float2(omr2, omr2), make_float2(1.0f, omr), ab);
+        const float omr = __fsub_rn(1.0f, ratio);
+        const float omr2 = __fmul_rn(omr, omr);
+        ab = __fadd2_rn(ab, make_float2(omr2, __fmul_rn(omr2, omr)));
     }
 }
 

@@ -776,6 +776,9 @@ __device__ __forceinline__ void density_one(int i, const Ctx &c, const float2 *_
             stencil_rows(key, start, g, ra, rl, c.n);
             if (rl[0] <= kMaskRow && rl[1] <= kMaskRow && rl[2] <= kMaskRow)
                 rec = make_int4(ra[0], ra[1], ra[2], kRowsMasked);
+            // the particle's own slot in its row (row 1): never a neighbour
+            // of itself (hash.c pairs distinct particles only)
+            const int self = i - ra[1];
 #pragma unroll
             for (int r = 0; r < 3; ++r) {
                 const float2 *row = pos + ra[r];
@@ -788,7 +791,7 @@ __device__ __forceinline__ void density_one(int i, const Ctx &c, const float2 *_
                     for (int t = 32 * hh; t < t1; ++t) {
                         float2 e;
                         const float r2 = dist2_packed(mp, __ldg(row + t), e);
-                        if (r2 <= h2) {
+                        if (r2 <= h2 && (r != 1 || t != self)) {
                             mh[hh] |= 1u << (t & 31);
                             add_density(ab, r2, h_recip);
                         }
@@ -799,15 +802,10 @@ __device__ __forceinline__ void density_one(int i, const Ctx &c, const float2 *_
                 for (int t = kMaskRow; t < len; ++t) {
                     float2 e;
                     const float r2 = dist2_packed(mp, __ldg(row + t), e);
-                    if (r2 <= h2) add_density(ab, r2, h_recip);
+                    if (r2 <= h2 && (r != 1 || t != self)) add_density(ab, r2, h_recip);
                 }
                 m[r] = ((unsigned long long)mh[1] << 32) | mh[0];
             }
-            // the particle met itself (r = 0) in its own row: remove it
-            ab.x -= 1.0f;
-            ab.y -= 1.0f;
-            const int self = i - ra[1];
-            if (self < kMaskRow) m[1] &= ~(1ull << self);
         } else {
             for_each_candidate(key, start, g, true, c.max_bucket, c.n, [&](int j) {
                 if (j == i) return;

@@ -118,36 +118,35 @@ k_features(Ctx c, const float2 *__restrict__ pos, const float2 *__restrict__ pre
         if (!capped) {
             int ra[3], rl[3];
             stencil_rows(key, start, g, ra, rl, c.n);
-            // one neighbour's terms: density, messages, counts (self
-            // included in rho and rho_near, removed below)
+            // one neighbour's terms (never the particle itself): density
+            // (add_density's rounding, so that the records equal the plain
+            // density pass's bit for bit), messages, counts
             auto visit = [&](int j, const float2 &q) {
                 float2 e;  // q - p
                 const float r2 = dist2_packed(mp, q, e);
                 const float rinv = rsqrtf(r2);
-                const float ratio = __fmul_rn(sqrt_approx(r2), h_recip);
-                const bool other = j != i;
-                count += other ? 1 : 0;
-                degenerate |= other && r2 <= 2e-12f;
+                const float ratio = __fmul_rn(__fsqrt_rn(r2), h_recip);
+                ++count;
+                degenerate |= r2 <= 2e-12f;
                 if (ratio < 1.0f) {
-                    const float omr = 1.0f - ratio;
-                    const float omr2 = omr * omr;
-                    ab = __ffma2_rn(make_float2(omr2, omr2), make_float2(1.0f, omr), ab);
-                    if (other) {
-                        // message sums in packed FP32x2 arithmetic
-                        const float2 u = __fmul2_rn(e, make_float2(rinv, rinv));
-                        const float2 w2 = make_float2(omr, omr);
-                        const float2 wu = __fmul2_rn(w2, u);
-                        V1 = __fadd2_rn(V1, wu);
-                        V2 = __ffma2_rn(make_float2(omr2, omr2), u, V2);
-                        Ms += omr;
-                        Tdiag = __ffma2_rn(wu, u, Tdiag);
-                        Txy += wu.x * u.y;
-                        // sum w (x_j - x_prev_j); the velocities follow at the end
-                        const float2 qp = __ldg(prev + j);
-                        Dsum = __ffma2_rn(w2, __fadd2_rn(q, make_float2(-qp.x, -qp.y)), Dsum);
-                    }
+                    const float omr = __fsub_rn(1.0f, ratio);
+                    const float omr2 = __fmul_rn(omr, omr);
+                    ab = __fadd2_rn(ab, make_float2(omr2, __fmul_rn(omr2, omr)));
+                    // message sums in packed FP32x2 arithmetic
+                    const float2 u = __fmul2_rn(e, make_float2(rinv, rinv));
+                    const float2 w2 = make_float2(omr, omr);
+                    const float2 wu = __fmul2_rn(w2, u);
+                    V1 = __fadd2_rn(V1, wu);
+                    V2 = __ffma2_rn(make_float2(omr2, omr2), u, V2);
+                    Ms += omr;
+                    Tdiag = __ffma2_rn(wu, u, Tdiag);
+                    Txy += wu.x * u.y;
+                    // sum w (x_j - x_prev_j); the velocities follow at the end
+                    const float2 qp = __ldg(prev + j);
+                    Dsum = __ffma2_rn(w2, __fadd2_rn(q, make_float2(-qp.x, -qp.y)), Dsum);
                 }
             };
+            const int self = i - ra[1];  // the particle's own slot in row 1
             if (rl[0] <= kMaskRow && rl[1] <= kMaskRow && rl[2] <= kMaskRow) {
                 rec = make_int4(ra[0], ra[1], ra[2], kRowsMasked);
                 // two phases, as the viscosity: the rows' hit masks from a
@@ -169,6 +168,7 @@ k_features(Ctx c, const float2 *__restrict__ pos, const float2 *__restrict__ pre
                     }
                     m[r] = ((unsigned long long)hi << 32) | lo;
                 }
+                m[1] &= ~(1ull << self);
 #pragma unroll
                 for (int r = 0; r < 3; ++r)
                     walk_mask<float2>(m[r], ra[r], c.n, [&](int j) { return __ldg(pos + j); }, visit);
@@ -180,18 +180,14 @@ k_features(Ctx c, const float2 *__restrict__ pos, const float2 *__restrict__ pre
                     for (int t = 0; t < rl[r]; ++t) {
                         const float2 q = __ldg(row + t);
                         float2 e;
-                        if (dist2_packed(mp, q, e) <= h2) {
-                            mr |= 1ull << (t & 63);
+                        if (dist2_packed(mp, q, e) <= h2 && (r != 1 || t != self)) {
+                            if (t < kMaskRow) mr |= 1ull << t;
                             visit(ra[r] + t, q);
                         }
                     }
                     m[r] = mr;
                 }
             }
-            ab.x -= 1.0f;
-            ab.y -= 1.0f;
-            const int self = i - ra[1];
-            if (self < kMaskRow) m[1] &= ~(1ull << self);
         } else {
             degenerate = true;
             for_each_candidate(key, start, g, true, c.max_bucket, c.n, [&](int j) {

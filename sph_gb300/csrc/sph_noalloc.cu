@@ -77,9 +77,13 @@ constexpr int kMaxDevices = 64;
 std::mutex g_setup_mu;
 void *g_scratch_addr[kMaxDevices] = {};
 
-// Device address of g_static_scratch on the current device, looked up once
-// per device (the host-side name of the array is only a stand-in).
-int scratch_address(void **out)
+// Device address of g_static_scratch on the current device (the host-side
+// name of the array is only a stand-in).  Looked up again on every call that
+// is not being captured into a graph, so that a context torn down and
+// recreated (cudaDeviceReset) is seen; a call under stream capture uses the
+// address of the last call on this device outside capture, which must
+// exist.
+int scratch_address(cudaStream_t stream, void **out)
 {
     int dev = 0;
     int rc = cuda_fail(cudaGetDevice(&dev), "cudaGetDevice");
@@ -88,12 +92,19 @@ int scratch_address(void **out)
         set_error("device ordinal %d above %d", dev, kMaxDevices - 1);
         return SPH_ERR_UNSUPPORTED;
     }
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    rc = cuda_fail(cudaStreamIsCapturing(stream, &cap), "cudaStreamIsCapturing");
+    if (rc != SPH_OK) return rc;
     std::lock_guard<std::mutex> lock(g_setup_mu);
-    if (!g_scratch_addr[dev]) {
+    if (cap == cudaStreamCaptureStatusNone) {
         void *p = nullptr;
         rc = cuda_fail(cudaGetSymbolAddress(&p, g_static_scratch), "cudaGetSymbolAddress");
         if (rc != SPH_OK) return rc;
         g_scratch_addr[dev] = p;
+    } else if (!g_scratch_addr[dev]) {
+        set_error("sph_cuda_density_static: the first call on a device must come before any "
+                  "stream capture");
+        return SPH_ERR_STATE;
     }
     *out = g_scratch_addr[dev];
     return SPH_OK;
@@ -131,10 +142,34 @@ k_static_scatter(int n, const int *__restrict__ ids, const float4 *__restrict__ 
     rho_near[id] = v.w;
 }
 
+// The counters of the last call's cell build, into caller device memory.
+__global__ void k_static_counters(sph_cuda_counters *out)
+{
+    const DevState *st = reinterpret_cast<const DevState *>(g_static_scratch + kOffState);
+    sph_cuda_counters c;
+    c.steps = 0ull;
+    c.out_of_grid = st->out_of_grid;
+    c.bucket_overflow = st->bucket_overflow;
+    c.max_cell_occupancy = st->max_occ;
+    c.list_cap_risk = st->list_cap_risk;
+    *out = c;
+}
+
 }  // namespace
 }  // namespace sph
 
 using namespace sph;
+
+extern "C" int sph_cuda_density_static_counters(sph_cuda_counters *d_out, void *stream)
+{
+    if (!d_out) {
+        set_error("sph_cuda_density_static_counters: null device output");
+        return SPH_ERR_INVALID;
+    }
+    // the kernel names the array itself: no device address is needed here
+    k_static_counters<<<1, 1, 0, static_cast<cudaStream_t>(stream)>>>(d_out);
+    return cuda_fail(cudaGetLastError(), "sph_cuda_density_static_counters launch");
+}
 
 extern "C" int sph_cuda_density_static(const float *x, const float *y, int n,
                                        const neighbor_grid_t *grid, const tunable_parameters *tp,
@@ -169,7 +204,7 @@ extern "C" int sph_cuda_density_static(const float *x, const float *y, int n,
         return SPH_ERR_INVALID;
     }
     void *base_v = nullptr;
-    int rc = scratch_address(&base_v);
+    int rc = scratch_address(static_cast<cudaStream_t>(stream), &base_v);
     if (rc != SPH_OK) return rc;
     if (n == 0) return SPH_OK;
 

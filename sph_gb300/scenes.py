@@ -356,6 +356,32 @@ def settle_and_drop(piles: list, steps: int = SETTLE_STEPS) -> list:
     return out
 
 
+def slab_columns(columns: int, nslabs: int) -> list:
+    """The 1-D x-slab decomposition of a lattice block of `columns` particle
+    columns over `nslabs` compute ranks, as partitionProblem
+    (geometry.c:101-160) cuts it: floor(columns / nslabs) columns each, the
+    remainder one more each to the leftmost slabs.  Returns [(first column,
+    number of columns)] per slab."""
+    equal = columns // nslabs
+    remaining = columns - equal * nslabs
+    out, first = [], 0
+    for s in range(nslabs):
+        length = equal + (1 if s < remaining else 0)
+        out.append((first, length))
+        first += length
+    return out
+
+
+def slab_indices(sc: Scene, slab: int, nslabs: int) -> np.ndarray:
+    """Particle indices of x-slab `slab` of a lattice-block scene (by the
+    particle's lattice column, as the reference assigns particles to ranks
+    at construction)."""
+    lat = sc.meta["lattice"]
+    first, length = slab_columns(int(lat["cols"]), nslabs)[slab]
+    col = np.arange(sc.n, dtype=np.int64) % int(lat["cols"])
+    return np.nonzero((col >= first) & (col < first + length))[0]
+
+
 def algorithmic_bytes_per_step(n: int, cells: int) -> int:
     """Canonical algorithmic HBM bytes of one step: 216 B per particle
     (viscosity+predict 40, cell build on predicted positions 68, density 16,

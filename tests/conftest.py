@@ -48,3 +48,17 @@ def bits_equal(a, b):
     a = np.ascontiguousarray(a, np.float32)
     b = np.ascontiguousarray(b, np.float32)
     return a.shape == b.shape and np.array_equal(a.view(np.int32), b.view(np.int32))
+
+
+def rel_ok(a, b, rtol=1e-5):
+    """Per element |a - b| <= rtol |b| with no absolute floor: where the
+    reference value is exactly zero (a particle with no neighbour) the result
+    must be an exact zero.  Returns (ok, largest relative error)."""
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    if a.shape != b.shape:
+        return False, float("inf")
+    err = np.abs(a - b)
+    nz = b != 0
+    rel = np.where(nz, err / np.where(nz, np.abs(b), 1.0), np.where(err == 0, 0.0, np.inf))
+    return bool(np.all(rel <= rtol)), float(rel.max(initial=0.0))

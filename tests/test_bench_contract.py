@@ -5,6 +5,8 @@ roofline fraction uses.  No call here touches a GPU."""
 import json
 import os
 
+import numpy as np
+
 import bench
 from sph_gb300 import scenes
 
@@ -45,13 +47,27 @@ def test_canonical_step_bytes():
     assert scenes.algorithmic_bytes_per_step(sc.n, sc.cells) == 216 * 4_194_304 + 16 * 6_444_050 == 1_009_074_464
 
 
+def test_slab_partition_is_the_references():
+    """partitionProblem (geometry.c:101-160): floor(columns / ranks) columns
+    each, the remainder to the leftmost ranks; the slabs cover every
+    particle exactly once."""
+    assert scenes.slab_columns(2393, 16)[:10] == [(150 * i, 150) for i in range(9)] + [(1350, 149)]
+    assert scenes.slab_columns(2393, 16)[-1] == (2244, 149)
+    sc = scenes.config2(n=65536)
+    parts = [scenes.slab_indices(sc, s, 8) for s in range(8)]
+    allidx = np.sort(np.concatenate(parts))
+    assert np.array_equal(allidx, np.arange(sc.n))
+    assert min(len(p) for p in parts) > 0
+
+
 def test_reference_arm_prints_the_contract_line(tmp_path):
-    """`bench.py --impl reference` on a tiny sample: one JSON line with the
-    reference arm's keys (it runs the CPU step only, no GPU)."""
+    """`bench.py --impl reference` on a small dam break: one JSON line with
+    the reference arm's keys (it runs the CPU step only, no GPU), on the
+    steps it was asked for."""
     import subprocess
     import sys
     out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
-                          "--cpu-sample", "4096", "--cpu-steps", "2"],
+                          "--n", "16384", "--steps", "2", "--warmup", "3"],
                          capture_output=True, text=True, timeout=600, cwd=ROOT)
     assert out.returncode == 0, out.stderr[-2000:]
     lines = [l for l in out.stdout.splitlines() if l.startswith("{")]
@@ -63,3 +79,4 @@ def test_reference_arm_prints_the_contract_line(tmp_path):
     assert d["cpu_baseline"]["kind"] in ("port", "reference")
     assert d["e2e"] == {"value": d["value"], "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}
+    assert d["steps"] == 2 and d["warmup"] == 3 and d["config"]["particles"] == 16384

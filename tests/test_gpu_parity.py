@@ -17,7 +17,7 @@ import numpy as np
 import pytest
 
 import oracle
-from conftest import EDGE_CONFIG, bits_equal, golden
+from conftest import EDGE_CONFIG, bits_equal, golden, rel_ok
 from sph_gb300 import PARTICLE_DTYPE, Simulation, scenes
 
 pytestmark = pytest.mark.gpu
@@ -71,11 +71,8 @@ def test_mover_scene_lists(cuda_lib):
 
 
 # ---------------------------------------------------------------- layer 2
-def _rel_ok(a, b, rtol=1e-5, atol=1e-7):
-    a = np.asarray(a, np.float64)
-    b = np.asarray(b, np.float64)
-    return np.all(np.abs(a - b) <= rtol * np.abs(b) + atol), float(
-        np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-30) * (np.abs(b) > 1e-3), initial=0))
+def _rel_ok(a, b, rtol=1e-5):
+    return rel_ok(a, b, rtol)
 
 
 @pytest.mark.parametrize("t", [100, 1000])
@@ -87,6 +84,18 @@ def test_density_matches_reference(cuda_lib, t):
     ok, err = _rel_ok(rho, g[f"h{t}_rho"])
     assert ok, err
     ok, err = _rel_ok(rhon, g[f"h{t}_rhon"])
+    assert ok, err
+
+
+@pytest.mark.parametrize("tag", ["sphere", "rect"])
+def test_density_mover_scene(cuda_lib, tag):
+    g = golden("mover")
+    sc = scenes.config2(n=4096)
+    with sim_for(g[f"{tag}_s100_x"], g[f"{tag}_s100_y"], config=sc.config()) as s:
+        rho, rhon = s.probe_density()
+    ok, err = _rel_ok(rho, g[f"{tag}_h100_rho"])
+    assert ok, err
+    ok, err = _rel_ok(rhon, g[f"{tag}_h100_rhon"])
     assert ok, err
 
 

@@ -48,6 +48,6 @@ def test_reference_arm_prints_on_rank0_only(capsys):
     import bench
 
     class A:
-        cpu_sample, cpu_steps, warmup, gpus = 1024, 2, 3, 2
+        n, steps, warmup, gpus = 16384, 2, 3, 2
     bench.run_reference(A, world=2, rank=1)
     assert capsys.readouterr().out == ""
