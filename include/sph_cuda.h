@@ -183,6 +183,19 @@ int sph_cuda_step(sph_cuda_t *h, const tunable_parameters *tp, int nsteps);
 /* Runs nsteps steps, step t using tps[t] (e.g. a moving mover); single scene. */
 int sph_cuda_step_schedule(sph_cuda_t *h, const tunable_parameters *tps, int nsteps);
 
+/* One step whose tunables change inside it, where the reference's compute
+ * rank receives them: apply_gravity, viscosity_impluses and
+ * predict_positions (fluid.c:273-279) run with tp_before (NULL keeps the
+ * current ones); then the MPI_Scatterv of fluid.c:293-294 delivers new
+ * tunables, and hash_fluid, double_density_relaxation, updateVelocities and
+ * the second hash (fluid.c:315-341) run with tp_after, which stay in force
+ * for the following steps.  Use it for the first sub-step of each frame
+ * (every steps_per_frame-th step) when the render rank sends tunables; the
+ * other steps keep sph_cuda_step.  Launched directly (not from the
+ * captured graph); single scene. */
+int sph_cuda_step_split(sph_cuda_t *h, const tunable_parameters *tp_before,
+                        const tunable_parameters *tp_after);
+
 /* Writes the particle state back through the caller's pointer array:
  * x_prev, y_prev, x, y, v_x, v_y, density, density_near, pressure,
  * pressure_near (a_x, a_y and id untouched).  Density and pressure are the

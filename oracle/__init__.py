@@ -118,6 +118,7 @@ def _load(kind: str):
         lib.orc_relax_f64.argtypes = [_P, _F, _F, _D, _D, _D]
         lib.orc_viscosity_f64.argtypes = [_P, _D, _D, _D]
         lib.orc_step_jacobi.argtypes = [_P, ctypes.c_int, _F, _D]
+        lib.orc_step_jacobi_split.argtypes = [_P, ctypes.POINTER(Tunables), ctypes.POINTER(Tunables)]
         lib.orc_diagnostics.argtypes = [_P, _D]
         lib.orc_cell_key.restype = ctypes.c_uint
         lib.orc_cell_key.argtypes = [ctypes.c_float, ctypes.c_float, ctypes.POINTER(SimConfig)]
@@ -192,6 +193,15 @@ class Sim:
         else:
             self._f("step")(self.h, nsteps, _fp(mv), _dp(diag))
         return diag
+
+    def step_jacobi_split(self, before: dict | None, after: dict):
+        """One float Jacobi step with the tunables switched after
+        predict_positions (fluid.c:293-294); `after` stays in force."""
+        if self.kind != "port":
+            raise ValueError("the Jacobi step exists only in the restatement")
+        b = None if before is None else ctypes.byref(tunables_from(before))
+        self.tun = tunables_from(after)
+        self.lib.orc_step_jacobi_split(self.h, b, ctypes.byref(self.tun))
 
     def get(self) -> dict:
         out = np.zeros((self.n, 12), np.float32)

@@ -26,15 +26,26 @@ from __future__ import annotations
 
 import numpy as np
 
+# The reference's constants, by source (tests/golden/liquid_shaders.json
+# holds them as read out of those sources, and the tests compare the two).
 TAPS = np.array([0.159576912161, 0.147308056121, 0.115876621105, 0.0776744219933,
                  0.0443683338718, 0.0215963866053, 0.00895781211794, 0.0044299121055113265],
-                np.float32)
+                np.float32)            # blur.frag:12-29: centre, then taps +-1 .. +-7
+BLUR_STEP = 0.004                      # vert_blur.vert / horz_blur.vert:13-26: texture units per tap
+SPRITE_DIAMETER = 0.020                # renderer.c:224: sprite diameter / screen width
+REDUCTION = 2                          # liquid_gl.c:44-48: texture size = screen / 2
+DISCARD_R2 = 0.34                      # liquid_particle.frag:14: discard r^2 above this
+INTENSITY = (1.0, 3.0)                 # liquid_particle.frag:19: 1.0 - 3.0 r^2
+COMPOSITE_DISCARD = 0.1                # render_liquid_texture.frag:11: discard alpha below
+ALPHA_EDGES = (0.1, 0.11)              # render_liquid_texture.frag:14: smoothstep of alpha
+WHITE_EDGES = (-0.15, -0.1)            # render_liquid_texture.frag:15: smoothstep of -alpha
+ALPHA_SCALE = 0.75                     # render_liquid_texture.frag:17: output alpha scale
 F = np.float32
 
 
 def splat(coords: np.ndarray, width: int, height: int) -> np.ndarray:
-    w, h = width // 2, height // 2
-    radius = F(0.5) * (F(width) * F(0.020) / F(2.0))
+    w, h = width // REDUCTION, height // REDUCTION
+    radius = F(0.5) * (F(width) * F(SPRITE_DIAMETER) / F(REDUCTION))
     inv = F(1.0) / radius
     acc = np.zeros((h, w), np.int64)
     reach = F(0.5831) * radius + F(1.0)
@@ -51,8 +62,8 @@ def splat(coords: np.ndarray, width: int, height: int) -> np.ndarray:
         dx = (xs.astype(np.float32) + F(0.5) - cx) * inv
         dy = (ys.astype(np.float32) + F(0.5) - cy) * inv
         r2 = dy[:, None] * dy[:, None] + dx[None, :] * dx[None, :]
-        v = np.rint((F(1.0) - F(3.0) * r2) * F(255.0)).astype(np.int64)
-        v[(r2 > F(0.34)) | (v < 0)] = 0
+        v = np.rint((F(INTENSITY[0]) - F(INTENSITY[1]) * r2) * F(255.0)).astype(np.int64)
+        v[(r2 > F(DISCARD_R2)) | (v < 0)] = 0
         acc[y0:y1 + 1, x0:x1 + 1] += v
     return np.minimum(acc, 255).astype(np.uint8)
 
@@ -74,7 +85,7 @@ def blur(tex: np.ndarray, vertical: bool) -> np.ndarray:
     pos = np.arange(length, dtype=np.float32)
     s = TAPS[0] * img.astype(np.float32)
     for k in range(1, 8):
-        o = F(0.004) * F(k) * F(length)
+        o = F(BLUR_STEP) * F(k) * F(length)
         s = s + TAPS[k] * (_lerp(img, pos - o) + _lerp(img, pos + o))
     out = np.clip(np.rint(s), 0, 255).astype(np.uint8)
     return out.T if vertical else out
@@ -103,9 +114,9 @@ def composite(a: np.ndarray, width: int, height: int) -> np.ndarray:
     au2, av2 = au[None, :], av[:, None]
     alpha = ((F(1.0) - av2) * ((F(1.0) - au2) * s00 + au2 * s01) +
              av2 * ((F(1.0) - au2) * s10 + au2 * s11)) / F(255.0)
-    o = F(0.75) * _smoothstep(0.1, 0.11, alpha)
-    white = _smoothstep(-0.15, -0.1, -alpha)
-    keep = alpha >= F(0.1)
+    o = F(ALPHA_SCALE) * _smoothstep(ALPHA_EDGES[0], ALPHA_EDGES[1], alpha)
+    white = _smoothstep(WHITE_EDGES[0], WHITE_EDGES[1], -alpha)
+    keep = alpha >= F(COMPOSITE_DISCARD)
     r = np.where(keep, white * o, F(0.0))
     b = np.where(keep, o, F(0.0))
     rgb = np.stack([r, r, b], axis=-1)

@@ -749,33 +749,58 @@ static void jacobi_relax(orc_sim *s, float *nx, float *ny)
 
 /* Same sequence as orc_step with the viscosity, density and relaxation
  * passes in gather (Jacobi) form: the formulation the CUDA library uses. */
+/* One float Jacobi step.  With `after`, the tunables are replaced after
+ * predict_positions and before the hash, the relaxation and the velocity
+ * update, where the reference's compute rank receives new tunables inside a
+ * step (the MPI_Scatterv of fluid.c:293-294). */
+static void jacobi_step(orc_sim *s, float *ta, float *tb, const orc_tunables *after)
+{
+    int i;
+    gs_gravity(s);
+    jacobi_viscosity(s, ta, tb);
+    memcpy(s->vx, ta, (size_t)s->n * sizeof(float));
+    memcpy(s->vy, tb, (size_t)s->n * sizeof(float));
+    gs_predict(s);
+    if (after) s->tp = *after;
+    orc_hash(s, 0);
+    jacobi_density(s);
+    jacobi_relax(s, ta, tb);
+    for (i = 0; i < s->n; i++) {
+        s->x[i] = ta[i];
+        s->y[i] = tb[i];
+    }
+    gs_update_velocities(s);
+    orc_hash(s, 0);
+}
+
 void orc_step_jacobi(void *h, int nsteps, const float *mover_xy, double *diag)
 {
     orc_sim *s = h;
     float *ta = malloc((size_t)s->n * sizeof(float));
     float *tb = malloc((size_t)s->n * sizeof(float));
-    int t, i;
+    int t;
     for (t = 0; t < nsteps; t++) {
         if (mover_xy) {
             s->tp.mover_center_x = mover_xy[2 * t];
             s->tp.mover_center_y = mover_xy[2 * t + 1];
         }
-        gs_gravity(s);
-        jacobi_viscosity(s, ta, tb);
-        memcpy(s->vx, ta, (size_t)s->n * sizeof(float));
-        memcpy(s->vy, tb, (size_t)s->n * sizeof(float));
-        gs_predict(s);
-        orc_hash(s, 0);
-        jacobi_density(s);
-        jacobi_relax(s, ta, tb);
-        for (i = 0; i < s->n; i++) {
-            s->x[i] = ta[i];
-            s->y[i] = tb[i];
-        }
-        gs_update_velocities(s);
-        orc_hash(s, 0);
+        jacobi_step(s, ta, tb, NULL);
         if (diag) diagnostics(s, diag + 3 * t);
     }
+    free(ta);
+    free(tb);
+}
+
+/* One Jacobi step whose tunables switch inside it: `before` (NULL keeps the
+ * current ones) for gravity, viscosity and prediction, `after` from the
+ * hash on, and for the steps that follow. */
+void orc_step_jacobi_split(void *h, const orc_tunables *before, const orc_tunables *after)
+{
+    orc_sim *s = h;
+    float *ta = malloc((size_t)s->n * sizeof(float));
+    float *tb = malloc((size_t)s->n * sizeof(float));
+    if (before) s->tp = *before;
+    jacobi_step(s, ta, tb, after);
     free(ta);
     free(tb);
 }

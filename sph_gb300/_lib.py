@@ -134,6 +134,8 @@ _SIGS = {
     "sph_cuda_upload_soa": (ctypes.c_int, [_P, c_float_p, c_float_p, c_float_p, c_float_p, ctypes.c_int]),
     "sph_cuda_step": (ctypes.c_int, [_P, ctypes.POINTER(TunableParameters), ctypes.c_int]),
     "sph_cuda_step_schedule": (ctypes.c_int, [_P, ctypes.POINTER(TunableParameters), ctypes.c_int]),
+    "sph_cuda_step_split": (ctypes.c_int, [_P, ctypes.POINTER(TunableParameters),
+                                           ctypes.POINTER(TunableParameters)]),
     "sph_cuda_download": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.POINTER(FluidParticle)), ctypes.c_int]),
     "sph_cuda_download_particles": (ctypes.c_int, [_P, _P, ctypes.c_int]),
     "sph_cuda_download_soa": (ctypes.c_int, [_P] + [c_float_p] * 6 + [ctypes.c_int]),

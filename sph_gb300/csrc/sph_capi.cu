@@ -659,6 +659,21 @@ int sph_cuda_step_schedule(sph_cuda_t *h, const tunable_parameters *tps, int nst
     return SPH_OK;
 }
 
+int sph_cuda_step_split(sph_cuda_t *h, const tunable_parameters *tp_before,
+                        const tunable_parameters *tp_after)
+{
+    SPH_TRY(check_handle(h));
+    if (h->nscenes != 1) {
+        set_error("a split step takes the tunables of one scene");
+        return SPH_ERR_INVALID;
+    }
+    SPH_TRY(validate_tp(tp_after));
+    SPH_TRY(apply_tp(h, tp_before));
+    if (h->n == 0) return set_scene_params(h, 0, tp_after);
+    int nk = 0;
+    return enqueue_step(h, nullptr, &nk, tp_after);
+}
+
 int sph_cuda_download(sph_cuda_t *h, fluid_particle *const *ptrs, int n)
 {
     SPH_TRY(check_handle(h));

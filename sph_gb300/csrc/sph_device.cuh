@@ -1,6 +1,8 @@
 // sph_device.cuh -- device helpers shared by the libsph_cuda kernels.
 #pragma once
 
+#include <climits>
+
 #include "sph_internal.h"
 
 namespace sph {
@@ -132,10 +134,6 @@ __device__ __forceinline__ float dist2(float dx, float dy)
     return __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
 }
 
-// dist2 of p and q in packed FP32x2 arithmetic (sm_100+): d = q - p per
-// component (given mp = -p), r2 = d.x^2 + d.y^2, each operation rounded
-// exactly as dist2(p.x - q.x, p.y - q.y) rounds it (the squares of +-dx
-// are equal), in three instructions instead of five.
 // One neighbour's share of (rho, rho_near): ((1 - r/h)^2, (1 - r/h)^3) for
 // r/h < 1 (calculate_density, fluid.c:527-539), each term rounded exactly as
 // the reference rounds it: r = sqrt(r2) correctly rounded (hash.c:190 takes
@@ -155,6 +153,10 @@ __device__ __forceinline__ void add_density(float2 &ab, float r2, float h_recip)
     }
 }
 
+// dist2 of p and q in packed FP32x2 arithmetic (sm_100+): d = q - p per
+// component (given mp = -p), r2 = d.x^2 + d.y^2, each operation rounded
+// exactly as dist2(p.x - q.x, p.y - q.y) rounds it (the squares of +-dx
+// are equal), in three instructions instead of five.
 __device__ __forceinline__ float dist2_packed(float2 mp, float2 q, float2 &d)
 {
     d = __fadd2_rn(q, mp);
@@ -266,6 +268,91 @@ __device__ __forceinline__ void stencil_rows(unsigned key, const int *__restrict
                 len[r] = 0;
         }
     }
+}
+
+// ---------------------------------------------------------------------------
+// CTA staging of stencil rows in shared memory
+// ---------------------------------------------------------------------------
+
+// The particles of a CTA are consecutive in cell order, so the stencil rows
+// its threads read are three short, heavily overlapping runs of slots: for
+// each row r, the union of the threads' ranges [lo, hi) is one contiguous run
+// a little longer than the CTA.  stage_rows copies those three runs of `src`
+// into shared memory once (coalesced 8- or 16-byte loads), so that every
+// neighbour read of the gather that follows is a shared-memory load instead
+// of an L1/L2 round trip.  Each thread passes its own ranges (lo = INT_MAX,
+// hi = INT_MIN for a row it does not read); every thread of the CTA must
+// call it (it has two CTA barriers).  Returns true when the runs fit `cap`
+// elements, in which case slot j of row r is at sm[j + delta[r]] (and, when
+// a second array src2 is given, at sm2[j + delta[r]]); otherwise nothing is
+// staged and the gather reads global memory as before.
+constexpr int kStageWarpsMax = kMaxBlock / 32;
+
+__device__ __forceinline__ int warp_min_i(int v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+__device__ __forceinline__ int warp_max_i(int v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+template <class T, class U = T>
+__device__ __forceinline__ bool stage_rows(const int (&lo)[3], const int (&hi)[3],
+                                           const T *__restrict__ src, T *sm, int cap,
+                                           int (&delta)[3], const U *__restrict__ src2 = nullptr,
+                                           U *sm2 = nullptr)
+{
+    __shared__ int4 s_red[kStageWarpsMax][2];  // per warp: (lo0, lo1, lo2, -), (hi0, hi1, hi2, -)
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int l[3], h[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        l[r] = warp_min_i(lo[r]);
+        h[r] = warp_max_i(hi[r]);
+    }
+    if (lane == 0) {
+        s_red[warp][0] = make_int4(l[0], l[1], l[2], 0);
+        s_red[warp][1] = make_int4(h[0], h[1], h[2], 0);
+    }
+    __syncthreads();
+    // every thread combines the per-warp words itself (no second reduction barrier)
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        l[r] = INT_MAX;
+        h[r] = INT_MIN;
+    }
+    for (int w = 0; w < nw; ++w) {
+        const int4 a = s_red[w][0], b = s_red[w][1];
+        l[0] = min(l[0], a.x); l[1] = min(l[1], a.y); l[2] = min(l[2], a.z);
+        h[0] = max(h[0], b.x); h[1] = max(h[1], b.y); h[2] = max(h[2], b.z);
+    }
+    int len[3], off[3], total = 0;
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        len[r] = h[r] > l[r] ? h[r] - l[r] : 0;
+        off[r] = total;
+        total += len[r];
+        delta[r] = off[r] - l[r];
+    }
+    const bool ok = total <= cap;  // the same in every thread of the CTA
+    if (ok) {
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+            for (int k = threadIdx.x; k < len[r]; k += blockDim.x) {
+                sm[off[r] + k] = src[l[r] + k];
+                if (src2) sm2[off[r] + k] = src2[l[r] + k];
+            }
+    }
+    // also when nothing was staged: s_red and sm are reused by the CTA's
+    // next call only after every thread has passed this barrier
+    __syncthreads();
+    return ok;
 }
 
 constexpr int kMaskRow = 64;  // candidates per stencil row recorded in a hit mask

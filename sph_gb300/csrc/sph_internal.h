@@ -198,7 +198,8 @@ int launch_upload_layout(sph_cuda *h, int n, const float *x, const float *y, con
                          const float *vy, const fluid_particle *recs);
 int launch_split_soa(sph_cuda *h, int n, const float2 *rec, float *out);
 int set_scene_params(sph_cuda *h, int scene, const tunable_parameters *tp);
-int enqueue_step(sph_cuda *h, cudaEvent_t *events, int *nkernels);
+int enqueue_step(sph_cuda *h, cudaEvent_t *events, int *nkernels,
+                 const tunable_parameters *mid_tp = nullptr);
 unsigned bounds_flags_kernels();  // checked builds (SPH_BOUNDS_CHECK): recorded index faults
 unsigned bounds_flags_learned();
 int enqueue_predicted_state(sph_cuda *h);       // first half of a step: C order + density

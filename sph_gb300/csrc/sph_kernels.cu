@@ -38,7 +38,22 @@
 #ifndef SPH_RELAX_MIN_BLOCKS
 #define SPH_RELAX_MIN_BLOCKS 4  // resident 256-thread CTAs per SM the relaxation is built for
 #endif
+#ifndef SPH_RELAX_SMEM
+#define SPH_RELAX_SMEM 0  // relaxation reads its stencil rows from a shared-memory copy
+#endif
+#ifndef SPH_DENS_SMEM
+#define SPH_DENS_SMEM 0   // density pass likewise
+#endif
+#ifndef SPH_VISC_SMEM
+#define SPH_VISC_SMEM 0   // viscosity pass likewise
+#endif
 namespace sph {
+// Shared-memory elements a gather CTA stages per thread of the CTA (the
+// three stencil-row runs of a CTA in one grid row are about 3.2 per thread).
+#ifndef SPH_STAGE_PER_THREAD
+#define SPH_STAGE_PER_THREAD 4
+#endif
+constexpr int kStagePerThread = SPH_STAGE_PER_THREAD;
 constexpr int kViscUnroll = SPH_VISC_UNROLL;
 constexpr int kDensUnroll = SPH_DENS_UNROLL;
 }  // namespace sph
@@ -751,61 +766,96 @@ k_viscosity_predict(Ctx c, const DevState *__restrict__ st, const float2 *__rest
 // Writes xr = (x, y, rho, rho_near) and, per stencil row, the bit mask of the
 // candidates that are neighbours (r2 <= h2, self excluded), which the
 // relaxation pass of the same positions walks instead of the whole stencil.
+// The candidate filter of one particle over its three stencil rows (slots
+// [ra[r], ra[r] + rl[r])), reading the rows from global memory or, SM, from
+// the CTA's shared-memory copy (slot j of row r at base[j + d[r]]).
+template <bool SM>
+__device__ __forceinline__ void density_filter(int i, float2 mp, float h2, float h_recip,
+                                               const int (&ra)[3], const int (&rl)[3],
+                                               const float2 *base, const int (&d)[3],
+                                               float2 &ab, unsigned long long (&m)[3])
+{
+    // the particle's own slot in its row (row 1): never a neighbour of
+    // itself (hash.c pairs distinct particles only)
+    const int self = i - ra[1];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        const float2 *row = base + ra[r] + (SM ? d[r] : 0);
+        auto at = [&](int t) { return SM ? row[t] : __ldg(row + t); };
+        const int len = rl[r];
+        unsigned mh[2] = {0u, 0u};  // 32-bit halves of the row's hit mask
+#pragma unroll
+        for (int hh = 0; hh < 2; ++hh) {
+            const int t1 = hh == 0 ? min(len, 32) : min(len, kMaskRow);
+#pragma unroll kDensUnroll
+            for (int t = 32 * hh; t < t1; ++t) {
+                float2 e;
+                const float r2 = dist2_packed(mp, at(t), e);
+                if (r2 <= h2 && (r != 1 || t != self)) {
+                    mh[hh] |= 1u << (t & 31);
+                    add_density(ab, r2, h_recip);
+                }
+            }
+        }
+        // rows longer than the mask (the relaxation then walks the whole
+        // stencil): the remaining candidates, no mask bits
+        for (int t = kMaskRow; t < len; ++t) {
+            float2 e;
+            const float r2 = dist2_packed(mp, at(t), e);
+            if (r2 <= h2 && (r != 1 || t != self)) add_density(ab, r2, h_recip);
+        }
+        m[r] = ((unsigned long long)mh[1] << 32) | mh[0];
+    }
+}
+
+// STAGED: every thread of the CTA calls this (also those with no particle,
+// valid = false), and the CTA first copies the union of its stencil rows to
+// shared memory `sm` (cap elements; stage_rows).
+template <bool STAGED = false>
 __device__ __forceinline__ void density_one(int i, const Ctx &c, const float2 *__restrict__ pos,
                                             const int *__restrict__ start, bool capped,
                                             float4 *__restrict__ xr_out,
                                             ulonglong2 *__restrict__ mask01,
                                             unsigned long long *__restrict__ mask2,
-                                            int4 *__restrict__ rows_out)
+                                            int4 *__restrict__ rows_out, bool valid = true,
+                                            float2 *sm = nullptr, int cap = 0)
 {
-    const Scene *S = c.scenes + scene_of(c, i);
+    const Scene *S = c.scenes + (valid ? scene_of(c, i) : 0);
     const SG g = load_grid(S);
     const float hh = __ldg(&S->P.smoothing_radius);
     const float h2 = __fmul_rn(hh, hh);
     const float h_recip = __fdiv_rn(1.0f, hh);
-    const float2 p = pos[i];
+    const float2 p = valid ? pos[i] : make_float2(-1.0f, -1.0f);
     const float2 mp = make_float2(-p.x, -p.y);
     const unsigned key = cell_key(p.x, p.y, g);
     float2 ab = make_float2(0.0f, 0.0f);  // (rho, rho_near)
     unsigned long long m[3] = {0ull, 0ull, 0ull};
     int4 rec = make_int4(0, 0, 0, kRowsNone);
-    if (searchable(key, i, start, g, capped, c.max_bucket)) {
+    const bool search = valid && searchable(key, i, start, g, capped, c.max_bucket);
+    int ra[3] = {0, 0, 0}, rl[3] = {0, 0, 0};
+    if (search && !capped) stencil_rows(key, start, g, ra, rl, c.n);
+    int d[3] = {0, 0, 0};
+    bool staged = false;
+    if (STAGED) {
+        int lo[3], hi[3];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            const bool use = search && !capped && rl[r] > 0;
+            lo[r] = use ? ra[r] : INT_MAX;
+            hi[r] = use ? ra[r] + rl[r] : INT_MIN;
+        }
+        staged = stage_rows(lo, hi, pos, sm, cap, d);
+    }
+    if (!valid) return;
+    if (search) {
         rec.w = kRowsFull;
         if (!capped) {
-            int ra[3], rl[3];
-            stencil_rows(key, start, g, ra, rl, c.n);
             if (rl[0] <= kMaskRow && rl[1] <= kMaskRow && rl[2] <= kMaskRow)
                 rec = make_int4(ra[0], ra[1], ra[2], kRowsMasked);
-            // the particle's own slot in its row (row 1): never a neighbour
-            // of itself (hash.c pairs distinct particles only)
-            const int self = i - ra[1];
-#pragma unroll
-            for (int r = 0; r < 3; ++r) {
-                const float2 *row = pos + ra[r];
-                const int len = rl[r];
-                unsigned mh[2] = {0u, 0u};  // 32-bit halves of the row's hit mask
-#pragma unroll
-                for (int hh = 0; hh < 2; ++hh) {
-                    const int t1 = hh == 0 ? min(len, 32) : min(len, kMaskRow);
-#pragma unroll kDensUnroll
-                    for (int t = 32 * hh; t < t1; ++t) {
-                        float2 e;
-                        const float r2 = dist2_packed(mp, __ldg(row + t), e);
-                        if (r2 <= h2 && (r != 1 || t != self)) {
-                            mh[hh] |= 1u << (t & 31);
-                            add_density(ab, r2, h_recip);
-                        }
-                    }
-                }
-                // rows longer than the mask (the relaxation then walks the
-                // whole stencil): the remaining candidates, no mask bits
-                for (int t = kMaskRow; t < len; ++t) {
-                    float2 e;
-                    const float r2 = dist2_packed(mp, __ldg(row + t), e);
-                    if (r2 <= h2 && (r != 1 || t != self)) add_density(ab, r2, h_recip);
-                }
-                m[r] = ((unsigned long long)mh[1] << 32) | mh[0];
-            }
+            if (STAGED && staged)
+                density_filter<true>(i, mp, h2, h_recip, ra, rl, sm, d, ab, m);
+            else
+                density_filter<false>(i, mp, h2, h_recip, ra, rl, pos, d, ab, m);
         } else {
             for_each_candidate(key, start, g, true, c.max_bucket, c.n, [&](int j) {
                 if (j == i) return;
@@ -820,6 +870,25 @@ __device__ __forceinline__ void density_one(int i, const Ctx &c, const float2 *_
     mask01[i] = make_ulonglong2(m[0], m[1]);
     mask2[i] = m[2];
     if (rows_out) rows_out[i] = rec;
+}
+
+// The density pass with the CTA's stencil rows staged in shared memory
+// (one tile of blockDim.x particles per CTA, or grid-stride over tiles).
+template <bool PERSIST>
+__global__ void __launch_bounds__(kMaxBlock, 4)
+k_density_sm(Ctx c, const float2 *__restrict__ pos, const int *__restrict__ start,
+             const unsigned *__restrict__ occ_in, float4 *__restrict__ xr_out,
+             ulonglong2 *__restrict__ mask01, unsigned long long *__restrict__ mask2,
+             int4 *__restrict__ rows_out)
+{
+    extern __shared__ float2 sm_pos[];
+    const bool capped = *occ_in > (unsigned)c.max_bucket;
+    const int ntiles = (c.n + blockDim.x - 1) / blockDim.x;
+    for (int tile = blockIdx.x; tile < ntiles; tile += PERSIST ? gridDim.x : ntiles) {
+        const int i = tile * blockDim.x + threadIdx.x;
+        density_one<true>(i, c, pos, start, capped, xr_out, mask01, mask2, rows_out, i < c.n,
+                          sm_pos, kStagePerThread * (int)blockDim.x);
+    }
 }
 
 // 32 registers (four 512-thread CTAs' worth per SM): full occupancy for this
@@ -940,6 +1009,14 @@ struct LearnedIn {
     bool defer = false;  // leave the fallback particles to a second pass
 };
 
+// Where a masked walk reads its neighbours' (x, y, rho, rho_near) records:
+// global memory, or the CTA's shared-memory copy of its stencil rows
+// (stage_rows: slot j of row r at sm[j + d[r]]).
+struct RowsIn {
+    const float4 *sm = nullptr;
+    int d[3] = {0, 0, 0};
+};
+
 template <bool PROBE, bool LEARNED = false, bool LONG_ROWS = false>
 __device__ __forceinline__ void relax_update_one(
     int i, const Ctx &cx, const float4 *__restrict__ xr, const ulonglong2 *__restrict__ mask01,
@@ -947,7 +1024,8 @@ __device__ __forceinline__ void relax_update_one(
     const float2 *__restrict__ prev, const int *__restrict__ ids, const int *__restrict__ start,
     bool capped, float2 *__restrict__ pos_out, float2 *__restrict__ vel_out,
     uint2 *__restrict__ kr_out, unsigned *__restrict__ cnt, float2 *__restrict__ probe_out,
-    const LearnedIn &L = LearnedIn(), bool *used_net = nullptr, int *tile_made = nullptr)
+    const LearnedIn &L = LearnedIn(), bool *used_net = nullptr, int *tile_made = nullptr,
+    const RowsIn &R = RowsIn())
 {
     const Scene *S = cx.scenes + scene_of(cx, i);
     const SG g = load_grid(S);
@@ -1031,13 +1109,25 @@ __device__ __forceinline__ void relax_update_one(
     if (mode == kRowsMasked) {
         const ulonglong2 m01 = mask01[i];
         const unsigned long long mm[3] = {m01.x, m01.y, mask2[i]};
+        if (R.sm) {
 #pragma unroll
-        for (int r = 0; r < 3; ++r)
-            walk_mask<float4>(
-                mm[r], ra[r], cx.n, [&](int j) { return __ldg(xr + j); },
-                [&](int j, const float4 &q) {
-                    relax_pair_walk(wc, p, q, i, j, S, ids, acc, nudges);
-                });
+            for (int r = 0; r < 3; ++r) {
+                const float4 *row = R.sm + R.d[r];
+                walk_mask<float4>(
+                    mm[r], ra[r], cx.n, [&](int j) { return row[j]; },
+                    [&](int j, const float4 &q) {
+                        relax_pair_walk(wc, p, q, i, j, S, ids, acc, nudges);
+                    });
+            }
+        } else {
+#pragma unroll
+            for (int r = 0; r < 3; ++r)
+                walk_mask<float4>(
+                    mm[r], ra[r], cx.n, [&](int j) { return __ldg(xr + j); },
+                    [&](int j, const float4 &q) {
+                        relax_pair_walk(wc, p, q, i, j, S, ids, acc, nudges);
+                    });
+        }
     } else if (mode == kRowsFull) {
         for_each_candidate(key, start, g, capped, cx.max_bucket, cx.n, [&](int j) {
             if (j == i) return;
@@ -1070,6 +1160,55 @@ __device__ __forceinline__ void relax_update_one(
     pos_out[i] = make_float2(nx, ny);
     vel_out[i] = make_float2(vx, vy);
     kr_out[i] = make_uint2(k2, rank);
+}
+
+
+// The slot ranges a thread's masked walk reads (stage_rows' lo, hi): for row
+// r, [ra[r], ra[r] + index of the highest hit + 1); nothing for rows without
+// hits or particles that do not walk masks.
+__device__ __forceinline__ void mask_ranges(int4 rw, unsigned long long m0, unsigned long long m1,
+                                            unsigned long long m2, int (&lo)[3], int (&hi)[3])
+{
+    const int ra[3] = {rw.x, rw.y, rw.z};
+    const unsigned long long mm[3] = {m0, m1, m2};
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        const bool use = rw.w == kRowsMasked && mm[r] != 0ull;
+        lo[r] = use ? ra[r] : INT_MAX;
+        hi[r] = use ? ra[r] + 64 - __clzll(mm[r]) : INT_MIN;
+    }
+}
+
+template <bool PROBE, bool PERSIST = false>
+__global__ void __launch_bounds__(kBlock, SPH_RELAX_MIN_BLOCKS)
+k_relax_update_sm(Ctx c, const float4 *__restrict__ xr, const ulonglong2 *__restrict__ mask01,
+                  const unsigned long long *__restrict__ mask2, const int4 *__restrict__ rows,
+                  const float2 *__restrict__ prev,
+                  const int *__restrict__ ids, const int *__restrict__ start,
+                  const unsigned *__restrict__ occ_in, unsigned *occ_reset,
+                  float2 *__restrict__ pos_out, float2 *__restrict__ vel_out,
+                  uint2 *__restrict__ kr_out, unsigned *__restrict__ cnt,
+                  float2 *__restrict__ probe_out)
+{
+    extern __shared__ float4 sm_rows[];
+    if (!PROBE && blockIdx.x == 0 && threadIdx.x == 0) *occ_reset = 0u;
+    const bool capped = *occ_in > (unsigned)c.max_bucket;
+    const int ntiles = (c.n + blockDim.x - 1) / blockDim.x;
+    for (int tile = blockIdx.x; tile < ntiles; tile += PERSIST ? gridDim.x : ntiles) {
+        const int i = tile * blockDim.x + threadIdx.x;
+        int lo[3] = {INT_MAX, INT_MAX, INT_MAX}, hi[3] = {INT_MIN, INT_MIN, INT_MIN};
+        if (i < c.n) {
+            const int4 rw = __ldg(rows + i);
+            const ulonglong2 m01 = __ldg(mask01 + i);
+            mask_ranges(rw, m01.x, m01.y, __ldg(mask2 + i), lo, hi);
+        }
+        RowsIn R;
+        if (stage_rows(lo, hi, xr, sm_rows, kStagePerThread * (int)blockDim.x, R.d)) R.sm = sm_rows;
+        if (i < c.n)
+            relax_update_one<PROBE>(i, c, xr, mask01, mask2, rows, prev, ids, start, capped,
+                                    pos_out, vel_out, kr_out, cnt, probe_out, LearnedIn(), nullptr,
+                                    nullptr, R);
+    }
 }
 
 template <bool PROBE, bool PERSIST = false>
@@ -1440,8 +1579,14 @@ static void enqueue_predict_sort(sph_cuda *h, Mark &mark)
 static void enqueue_density(sph_cuda *h)
 {
     DevState *st = h->d_state;
+#if SPH_DENS_SMEM
+    auto kd = h->shape[1].persistent ? k_density_sm<true> : k_density_sm<false>;
+    const size_t smem = (size_t)kStagePerThread * h->shape[1].block * sizeof(float2);
+#else
     auto kd = h->shape[1].persistent ? k_density_t<true> : k_density_t<false>;
-    kd<<<gather_grid(h, h->shape[1]), h->shape[1].block, 0, h->stream>>>(
+    const size_t smem = 0;
+#endif
+    kd<<<gather_grid(h, h->shape[1]), h->shape[1].block, smem, h->stream>>>(
         make_ctx(h), h->pos_c, h->start_c, &st->build_max_occ[SLOT_PREDICTED], h->xr_c,
         h->mask01_c, h->mask2_c, h->rows_c);
 }
@@ -1495,8 +1640,13 @@ int launch_learned_relax(sph_cuda *h, float2 *probe_out, cudaEvent_t *events)
 }
 
 // Queues one step.  With `events` (one per kernel + 1) each kernel is
-// bracketed for timing.
-int enqueue_step(sph_cuda *h, cudaEvent_t *events, int *nkernels)
+// bracketed for timing.  With `mid_tp`, the scene's tunables are replaced
+// by *mid_tp after the first half (gravity, viscosity, prediction and the
+// cell build of the predicted positions) and before the density pass, the
+// relaxation and the velocity update -- where the reference's compute rank
+// receives new tunables inside a step (fluid.c:293-294, between
+// predict_positions at :279 and hash_fluid at :315).  Single-scene handles.
+int enqueue_step(sph_cuda *h, cudaEvent_t *events, int *nkernels, const tunable_parameters *mid_tp)
 {
     const int n = h->n;
     const int nb = blocks_for(n);
@@ -1509,6 +1659,10 @@ int enqueue_step(sph_cuda *h, cudaEvent_t *events, int *nkernels)
     };
     mark();
     enqueue_predict_sort(h, mark);
+    if (mid_tp) {
+        const int rc = set_scene_params(h, 0, mid_tp);
+        if (rc != SPH_OK) return rc;
+    }
     if (h->learned) {
         int rc = launch_learned_passes(h, events ? events + e : nullptr);
         if (rc != SPH_OK) return rc;
@@ -1519,8 +1673,15 @@ int enqueue_step(sph_cuda *h, cudaEvent_t *events, int *nkernels)
     } else {
         enqueue_density(h);
         mark();
+#if SPH_RELAX_SMEM
+        auto kr = h->shape[2].persistent ? k_relax_update_sm<false, true>
+                                         : k_relax_update_sm<false, false>;
+        const size_t smem = (size_t)kStagePerThread * h->shape[2].block * sizeof(float4);
+#else
         auto kr = h->shape[2].persistent ? k_relax_update<false, true> : k_relax_update<false, false>;
-        kr<<<gather_grid(h, h->shape[2]), h->shape[2].block, 0, h->stream>>>(
+        const size_t smem = 0;
+#endif
+        kr<<<gather_grid(h, h->shape[2]), h->shape[2].block, smem, h->stream>>>(
             c, h->xr_c, h->mask01_c, h->mask2_c, h->rows_c, h->prev_c, h->id_c, h->start_c,
             &st->build_max_occ[SLOT_PREDICTED], &st->build_max_occ[SLOT_RELAXED], h->pos_b,
             h->vel_b, h->kr_b, h->cnt, nullptr);

@@ -6,10 +6,12 @@
  * tunables, a 15 x 15/aspect box, h = 2 x the initial particle spacing, a
  * 100-particle bucket cap and 400-entry lists), the particles live in the
  * caller's AoS array behind a pointer array as in fluid.c:183-197, and each
- * step is one sph_cuda_step.  Every steps_per_frame-th step the packed
- * short coordinates (fluid.c:356-364) go to the stand-in render rank on a
- * copy stream, and the stand-in answers the previous frame with tunables
- * for the following steps (fluid.c:293-294): it moves
+ * step is one sph_cuda_step.  The last sub-step of every frame is a split
+ * step (sph_cuda_step_split): after its prediction the stand-in render rank
+ * hands over new tunables, as the reference's MPI_Scatterv does in that
+ * sub-step (fluid.c:293-294), and at its end the packed short coordinates
+ * (fluid.c:356-364) go to the stand-in on a copy stream, overlapping the
+ * next frame's steps as the reference's MPI_Isend does.  The stand-in moves
  * the mover along the render rank's inactive-mode path (renderer.c:493-532)
  * and cycles the fluid presets x, y, a, b (controls.c:344-401) every
  * `preset_frames` frames.
@@ -17,7 +19,10 @@
  * usage: sph_compute_rank N STEPS STEPS_PER_FRAME OUT_PREFIX [PIX_X PIX_Y [PRESET_FRAMES]]
  *
  * Writes OUT_PREFIX.init     n x (x, y) float32: the uploaded particles
- *        OUT_PREFIX.tunables STEPS x tunable_parameters: each step's tunables
+ *        OUT_PREFIX.tunables STEPS x 2 tunable_parameters: each step's
+ *                            tunables before and after the point where a
+ *                            frame's new ones arrive (equal except in the
+ *                            last sub-step of a frame)
  *        OUT_PREFIX.frames   header (int32 n, int32 frames, float32 max_x,
  *                            max_y, h, uint32 size_x, size_y) then frames x
  *                            n x 2 int16 coordinates
@@ -46,20 +51,26 @@ typedef struct {
     int preset_frames;
 } render_standin;
 
-/* Receives one frame of coordinates and returns the tunables the compute
- * rank uses from the next step on. */
-static int render_frame(render_standin *r, const short *coords, int n, float max_x, float max_y,
-                        tunable_parameters *tp)
+/* The render rank's tunables for the frame ending now (its MPI_Scatterv,
+ * renderer.c:268): the next preset every `preset_frames` frames, and the
+ * mover one step further along the inactive-mode path. */
+static int render_tunables(render_standin *r, float max_x, float max_y, tunable_parameters *tp)
 {
-    if (fwrite(coords, sizeof(short), 2 * (size_t)n, r->frames) != 2 * (size_t)n) return 1;
-    ++r->nframes;
-    if (r->preset_frames > 0 && r->nframes % r->preset_frames == 0) {
+    if (r->preset_frames > 0 && r->nframes > 0 && r->nframes % r->preset_frames == 0) {
         static const char cycle[4] = {'x', 'y', 'a', 'b'};
         if (sph_cuda_tunables_preset(tp, cycle[(r->nframes / r->preset_frames) % 4]) != SPH_OK)
             return 1;
     }
     return sph_cuda_mover_track(max_x, max_y, &r->gl_x, &r->direction, &tp->mover_center_x,
                                 &tp->mover_center_y) != SPH_OK;
+}
+
+/* Receives one frame of coordinates (the render rank's Irecv, renderer.c:276-282). */
+static int render_receive(render_standin *r, const short *coords, int n)
+{
+    if (fwrite(coords, sizeof(short), 2 * (size_t)n, r->frames) != 2 * (size_t)n) return 1;
+    ++r->nframes;
+    return 0;
 }
 
 int main(int argc, char **argv)
@@ -187,27 +198,32 @@ int main(int argc, char **argv)
     for (int t = 0; t < steps; ++t) {
         if (tp->kill_sim) break;
         fwrite(tp, sizeof(*tp), 1, ftp);
-        if (sph_cuda_step(sim, tp, 1) != SPH_OK) return fail("step");
         if (sub_step == steps_per_frame - 1) {
-            if (pending >= 0) {  /* the previous frame: arrived while this one ran */
+            /* the previous frame's coordinates have arrived at the render
+             * rank (its copy overlapped this frame's steps); it answers with
+             * this frame's tunables, which act from the hash of this
+             * sub-step on */
+            if (pending >= 0) {
                 if (sph_cuda_coords_wait(sim, coords[pending]) != SPH_OK) return fail("wait");
-                if (render_frame(&r, coords[pending], n, box.max_x, box.max_y, tp)) {
-                    fprintf(stderr, "compute_rank: render stand-in failed\n");
-                    return 1;
-                }
+                if (render_receive(&r, coords[pending], n)) return fail("render stand-in");
             }
+            tunable_parameters after = *tp;
+            if (render_tunables(&r, box.max_x, box.max_y, &after)) return fail("render stand-in");
+            fwrite(&after, sizeof(after), 1, ftp);
+            if (sph_cuda_step_split(sim, tp, &after) != SPH_OK) return fail("split step");
+            *tp = after;
             pending = frame & 1;
             if (sph_cuda_pack_coords_async(sim, coords[pending], n) != SPH_OK) return fail("pack");
             ++frame;
+        } else {
+            fwrite(tp, sizeof(*tp), 1, ftp);
+            if (sph_cuda_step(sim, tp, 1) != SPH_OK) return fail("step");
         }
         sub_step = sub_step == steps_per_frame - 1 ? 0 : sub_step + 1;
     }
     if (pending >= 0) {
         if (sph_cuda_coords_wait(sim, coords[pending]) != SPH_OK) return fail("wait");
-        if (render_frame(&r, coords[pending], n, box.max_x, box.max_y, tp)) {
-            fprintf(stderr, "compute_rank: render stand-in failed\n");
-            return 1;
-        }
+        if (render_receive(&r, coords[pending], n)) return fail("render stand-in");
     }
     if (sph_cuda_download(sim, ptrs, n) != SPH_OK) return fail("download");
     double diag[3];

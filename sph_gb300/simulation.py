@@ -156,6 +156,14 @@ class Simulation:
         arr = (ctypes.c_int * 6)(*[int(v) for v in shapes])
         check(lib().sph_cuda_set_launch_shapes(self._h, arr))
 
+    def step_split(self, before: dict | None, after: dict):
+        """One step whose tunables switch after the prediction, where the
+        reference's compute rank receives new ones (sph_cuda_step_split);
+        `after` stays in force (and becomes this object's params)."""
+        b = None if before is None else ctypes.byref(tunables(before))
+        check(lib().sph_cuda_step_split(self._h, b, ctypes.byref(tunables(after))))
+        self.params = dict(after)
+
     def step_schedule(self, params_list: list):
         arr = (_lib.TunableParameters * len(params_list))(*[tunables(p) for p in params_list])
         check(lib().sph_cuda_step_schedule(self._h, arr, len(params_list)))

@@ -190,3 +190,25 @@ def test_jacobi_drift_within_gate_cpu():
     for col in (0, 2):
         assert abs(d[-1, col] - g[-1, col]) / g[-1, col] < 0.02
         assert abs(d[:, col].mean() - g[:, col].mean()) / g[:, col].mean() < 0.02
+
+
+def test_split_jacobi_step_is_the_step_when_tunables_stay():
+    """The oracle's split step (tunables replaced after predict_positions,
+    where fluid.c:293-294 receives them) equals its plain Jacobi step bit
+    for bit when nothing changes, and differs when the mover and viscosity
+    change mid-step."""
+    sc = scenes.config2(n=4096)
+    P, C = sc.params.as_dict(), sc.config()
+    a = oracle.Sim("port", sc.x, sc.y, sc.vx, sc.vy, P, C)
+    b = oracle.Sim("port", sc.x, sc.y, sc.vx, sc.vy, P, C)
+    a.step(3, jacobi=True)
+    for _ in range(3):
+        b.step_jacobi_split(P, P)
+    sa, sb = a.get(), b.get()
+    for k in ("x", "y", "v_x", "v_y"):
+        assert bits_equal(sa[k], sb[k]), k
+    Q = dict(P, sigma=1.0, mover_center_x=P["mover_center_x"] + 2.0)
+    a.step_jacobi_split(P, Q)
+    b.set_params(Q)
+    b.step(1, jacobi=True)
+    assert not bits_equal(a.get()["x"], b.get()["x"])

@@ -1,6 +1,7 @@
 """The CPU restatement of the liquid image (oracle/liquid_image.py): sanity
 of each pass on hand-made inputs (no GPU)."""
 import numpy as np
+import pytest
 
 from oracle import liquid_image as li
 
@@ -38,3 +39,47 @@ def test_composite_threshold():
     a[:] = 200  # 0.78: opaque blue-ish, no white
     rgb = li.composite(a, 40, 20)
     assert (rgb[..., 2] == 191).all() and (rgb[..., 0] == 0).all()
+
+
+def _fixture():
+    import json
+    import os
+    with open(os.path.join(os.path.dirname(__file__), "golden", "liquid_shaders.json")) as f:
+        return json.load(f)
+
+
+def test_restatement_uses_the_reference_shader_constants():
+    """Every constant of the restatement equals the one read out of the
+    reference's shaders and render code (tests/golden/liquid_shaders.json,
+    written by tests/golden/make_shader_constants.py)."""
+    c = _fixture()
+    w = np.array(c["blur_weights_in_tap_order"], np.float32)
+    assert c["blur_tap_order"][7] == "centre" and len(w) == 15
+    assert np.array_equal(w[7], li.TAPS[0])
+    assert np.array_equal(w[8:], li.TAPS[1:]) and np.array_equal(w[:7][::-1], li.TAPS[1:])
+    steps = np.concatenate([np.arange(-7, 0), np.arange(1, 8)]) * li.BLUR_STEP
+    for k in ("vertical_offsets", "horizontal_offsets"):
+        assert np.allclose(c[k], steps, rtol=0, atol=1e-12), k
+    for k in ("vertical_cross_offsets", "horizontal_cross_offsets"):
+        assert not np.any(c[k]), k
+    assert c["sprite_discard_r2"] == li.DISCARD_R2
+    assert tuple(c["sprite_intensity"]) == li.INTENSITY
+    assert c["composite_discard_alpha"] == li.COMPOSITE_DISCARD
+    assert tuple(c["composite_alpha_edges"]) == li.ALPHA_EDGES
+    assert tuple(c["composite_white_edges"]) == li.WHITE_EDGES
+    assert c["composite_alpha_scale"] == li.ALPHA_SCALE
+    assert c["sprite_diameter_per_screen_width"] == li.SPRITE_DIAMETER
+    assert c["texture_reduction"] == li.REDUCTION
+
+
+def test_shader_fixture_matches_the_reference_sources():
+    """Where the reference checkout is present, its sources still give the
+    committed fixture."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
+    import make_shader_constants as m
+    root = m.default_reference_root()
+    if not os.path.isdir(os.path.join(root, "shaders")):
+        pytest.skip("reference sources not present on this machine")
+    assert m.read_constants(root) == _fixture()
