@@ -21,9 +21,24 @@ __device__ __forceinline__ int scene_of(const Ctx &c, int i)
     return lo;
 }
 
-// A scene's grid, as the cell keys and stencils use it.
+// Programmatic dependent launch between the kernels of a step: a kernel
+// lets the next one start launching as soon as all of its own CTAs are
+// running (pdl_trigger), and waits for its predecessor's results before
+// touching them (pdl_wait).  Both are no-ops for a kernel launched without
+// the programmatic-serialization attribute.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;"); }
+__device__ __forceinline__ void pdl_enter()
+{
+    pdl_wait();
+    pdl_trigger();
+}
+
+// A scene's grid, as the cell keys and stencils use it.  inv is 1/spacing
+// when spacing is a power of two (then x / spacing == x * inv exactly: both
+// round the same real number), 0 otherwise.
 struct SG {
-    float spacing;
+    float spacing, inv;
     int size_x, size_y, ncells, c_off;
 };
 
@@ -31,6 +46,11 @@ __device__ __forceinline__ SG load_grid(const Scene *__restrict__ S)
 {
     SG g;
     g.spacing = __ldg(&S->spacing);
+    const unsigned b = __float_as_uint(g.spacing);
+    const unsigned e = (b >> 23) & 0xFFu;
+    // a normal power of two whose reciprocal is normal too
+    g.inv = ((b & 0x807FFFFFu) == 0u && e > 1u && e < 253u) ? __uint_as_float((254u - e) << 23)
+                                                           : 0.0f;
     g.size_x = __ldg(&S->size_x);
     g.size_y = __ldg(&S->size_y);
     g.ncells = __ldg(&S->ncells);
@@ -62,8 +82,9 @@ __device__ __forceinline__ tunable_parameters load_params(const Scene *__restric
 // scene's "no cell" bucket c_off + ncells.
 __device__ __forceinline__ unsigned cell_key(float x, float y, const SG &g)
 {
-    const float fx = floorf(__fdiv_rn(x, g.spacing));
-    const float fy = floorf(__fdiv_rn(y, g.spacing));
+    const bool p2 = g.inv != 0.0f;
+    const float fx = floorf(p2 ? __fmul_rn(x, g.inv) : __fdiv_rn(x, g.spacing));
+    const float fy = floorf(p2 ? __fmul_rn(y, g.inv) : __fdiv_rn(y, g.spacing));
     if (!(fx >= 0.0f) || !(fy >= 0.0f) || fx > 1073741824.0f || fy > 1073741824.0f)
         return (unsigned)(g.c_off + g.ncells);
     const long long k = (long long)(unsigned)fy * g.size_x + (long long)(unsigned)fx;

@@ -22,6 +22,8 @@
 // used solely to give each particle a distinct scratch slot; the final
 // in-cell order is by id, recomputed deterministically in `permute`.
 #include <algorithm>
+#include <type_traits>
+#include <utility>
 #include <cstdio>
 
 #include "sph_device.cuh"
@@ -47,6 +49,7 @@
 #ifndef SPH_VISC_SMEM
 #define SPH_VISC_SMEM 0   // viscosity pass likewise
 #endif
+
 namespace sph {
 // Shared-memory elements a gather CTA stages per thread of the CTA (the
 // three stencil-row runs of a CTA in one grid row are about 3.2 per thread).
@@ -331,6 +334,7 @@ k_cell_starts(unsigned *__restrict__ in, int M, const unsigned *__restrict__ noc
     static_assert(ITEMS % 4 == 0 && (ITEMS == 16 || ITEMS % 32 == 0), "items per thread");
     __shared__ unsigned sh_sum[WARPS], sh_pre[WARPS], sh_m[WARPS];
     __shared__ unsigned long long sh_e[WARPS], sh_o[WARPS];
+    pdl_enter();
     const int tile = blockIdx.x;
     const int base = tile * kBuildTile + threadIdx.x * ITEMS;
     // prefix of all earlier tiles, from the producers' counts: the loads go
@@ -349,10 +353,16 @@ k_cell_starts(unsigned *__restrict__ in, int M, const unsigned *__restrict__ noc
             for (int j = 0; j < kBatch; ++j) acc += x[j];
         }
     }
-    const unsigned expect = threadIdx.x == 0 ? __ldcg(tile_cnt + tile) : 0u;
+    // a tile no producer counted a particle into holds only zero counters:
+    // its counters are neither read nor zeroed again (most tiles of a
+    // sparse scene); the others check their total against the count below
+    const unsigned expect = __ldcg(tile_cnt + tile);
     unsigned v[ITEMS];
     const bool full = base + ITEMS <= M;
-    if (full) {
+    if (expect == 0u) {
+#pragma unroll
+        for (int e = 0; e < ITEMS; ++e) v[e] = 0u;
+    } else if (full) {
         const uint4 *p = reinterpret_cast<const uint4 *>(in + base);
 #pragma unroll
         for (int q = 0; q < ITEMS / 4; ++q) {
@@ -417,7 +427,7 @@ k_cell_starts(unsigned *__restrict__ in, int M, const unsigned *__restrict__ noc
             t.z = (int)run; run += v[4 * q + 2];
             t.w = (int)run; run += v[4 * q + 3];
             o[q] = t;
-            z[q] = make_uint4(0, 0, 0, 0);
+            if (expect != 0u) z[q] = make_uint4(0, 0, 0, 0);
         }
     } else {
 #pragma unroll
@@ -425,7 +435,7 @@ k_cell_starts(unsigned *__restrict__ in, int M, const unsigned *__restrict__ noc
             if (base + e < M) {
                 out[base + e] = (int)run;
                 run += v[e];
-                in[base + e] = 0u;
+                if (expect != 0u) in[base + e] = 0u;
             }
         }
     }
@@ -510,6 +520,7 @@ k_scatter_ids_x(int n, const uint2 *__restrict__ kr, const int *__restrict__ id_
                 const int *__restrict__ start, int *__restrict__ tmp, unsigned *tile_cnt,
                 int ntiles)
 {
+    pdl_enter();
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     for (int t = g; t < ntiles; t += gridDim.x * blockDim.x) tile_cnt[t] = 0u;
     const int i0 = blockIdx.x * blockDim.x * K + threadIdx.x;
@@ -542,6 +553,7 @@ k_permute_x(int n, const uint2 *__restrict__ kr, const int *__restrict__ start,
             int *__restrict__ id_dst, float2 *__restrict__ a_dst, float2 *__restrict__ b_dst,
             DevState *__restrict__ end_step)
 {
+    pdl_enter();
     if (end_step && blockIdx.x == 0 && threadIdx.x == 0) {
         end_step->lists_valid = 1u;
         end_step->steps += 1ull;
@@ -609,14 +621,19 @@ k_keys(Ctx c, const float2 *__restrict__ pos, uint2 *__restrict__ kr, unsigned *
 // I_ij = dt (1 - r/h)(sigma u + beta u^2) (x_j - x_i)/r for u > 0,
 // u = ((v_i - v_j).(x_j - x_i))/r, all from the velocities after gravity.
 // PROBE writes dv instead of advancing.
-template <bool PROBE>
+// STAGED: every thread of the CTA calls this (valid = false for a thread
+// without a particle), and the CTA first copies the union of its stencil
+// rows' positions and velocities to shared memory (sm_p, sm_v; cap
+// elements each; stage_rows).
+template <bool PROBE, bool STAGED = false>
 __device__ __forceinline__ void viscosity_predict_one(
     int i, const Ctx &c, const DevState *__restrict__ st, const float2 *__restrict__ pos,
     const float2 *__restrict__ vel, const int *__restrict__ start, bool capped,
     float2 *__restrict__ pos_out, float2 *__restrict__ prev_out, uint2 *__restrict__ kr_out,
-    unsigned *__restrict__ cnt, float2 *__restrict__ probe_out, int *tile_made = nullptr)
+    unsigned *__restrict__ cnt, float2 *__restrict__ probe_out, int *tile_made = nullptr,
+    bool valid = true, float2 *sm_p = nullptr, float2 *sm_v = nullptr, int cap = 0)
 {
-    const Scene *S = c.scenes + scene_of(c, i);
+    const Scene *S = c.scenes + (valid ? scene_of(c, i) : 0);
     const SG g = load_grid(S);
     const float dt = __ldg(&S->P.time_step);
     const float gdt = __fmul_rn(-__ldg(&S->P.g), dt);
@@ -626,8 +643,8 @@ __device__ __forceinline__ void viscosity_predict_one(
     const float sigma = __ldg(&S->P.sigma), beta = __ldg(&S->P.beta);
     const float dt_h = dt * h_recip;
 
-    const float2 p = pos[i];
-    const float2 v0 = vel[i];  // before gravity: velocity differences need none
+    const float2 p = valid ? pos[i] : make_float2(-1.0f, -1.0f);
+    const float2 v0 = valid ? vel[i] : make_float2(0.0f, 0.0f);  // before gravity: velocity differences need none
     float2 v = make_float2(v0.x, __fadd_rn(v0.y, gdt));
     float2 dv = make_float2(0.0f, 0.0f);
     const unsigned key = cell_key(p.x, p.y, g);
@@ -666,47 +683,77 @@ __device__ __forceinline__ void viscosity_predict_one(
         return make_float4(q.x, q.y, w.x, w.y);
     };
     auto impulse = [&](int j) { impulse_with(load_pv(j)); };
-    if ((PROBE || st->lists_valid) && searchable(key, i, start, g, capped, c.max_bucket)) {
-        bool walked = false;
-        if (!capped) {
-            // two phases: a cheap scan marks the neighbours of each stencil
-            // row, then only they pay for the impulse (less SIMT waste)
-            int ra[3], rl[3];
-            stencil_rows(key, start, g, ra, rl, c.n);
-            if (rl[0] <= kMaskRow && rl[1] <= kMaskRow && rl[2] <= kMaskRow) {
-                unsigned long long m[3];
+    const bool search = valid && (PROBE || st->lists_valid) &&
+                        searchable(key, i, start, g, capped, c.max_bucket);
+    int ra[3] = {0, 0, 0}, rl[3] = {0, 0, 0};
+    if (search && !capped) stencil_rows(key, start, g, ra, rl, c.n);
+    const bool masked = search && !capped && rl[0] <= kMaskRow && rl[1] <= kMaskRow &&
+                        rl[2] <= kMaskRow;
+    int d[3] = {0, 0, 0};
+    bool staged = false;
+    if (STAGED) {
+        int lo[3], hi[3];
 #pragma unroll
-                for (int r = 0; r < 3; ++r) {
-                    const float2 *row = pos + ra[r];
-                    const int len = rl[r];
-                    // 32-bit halves: cheaper bit operations than one 64-bit mask
-                    unsigned lo = 0u, hi = 0u;
-                    const int n0 = min(len, 32);
-#pragma unroll kViscUnroll
-                    for (int t = 0; t < n0; ++t) {
-                        float2 e;
-                        const float r2 = dist2_packed(mp, __ldg(row + t), e);
-                        // self and coincident particles are marked too; the
-                        // impulse skips them (r2 == 0)
-                        lo |= (unsigned)(r2 <= h2) << t;
-                    }
-#pragma unroll kViscUnroll
-                    for (int t = 32; t < len; ++t) {
-                        float2 e;
-                        const float r2 = dist2_packed(mp, __ldg(row + t), e);
-                        hi |= (unsigned)(r2 <= h2) << (t - 32);
-                    }
-                    m[r] = ((unsigned long long)hi << 32) | lo;
-                }
-                m[1] &= ~(1ull << (i - ra[1]));  // self
-#pragma unroll
-                for (int r = 0; r < 3; ++r)
-                    walk_mask<float4>(m[r], ra[r], c.n, load_pv,
-                                      [&](int, const float4 &d) { impulse_core(d, true); });
-                walked = true;
-            }
+        for (int r = 0; r < 3; ++r) {
+            const bool use = masked && rl[r] > 0;
+            lo[r] = use ? ra[r] : INT_MAX;
+            hi[r] = use ? ra[r] + rl[r] : INT_MIN;
         }
-        if (!walked) for_each_candidate(key, start, g, capped, c.max_bucket, c.n, impulse);
+        staged = stage_rows(lo, hi, pos, sm_p, cap, d, vel, sm_v);
+    }
+    if (!valid) return;
+    if (masked) {
+        // two phases: a cheap scan marks the neighbours of each stencil
+        // row, then only they pay for the impulse (less SIMT waste)
+        auto two_phase = [&](auto SMc, const float2 *bp, const float2 *bv) {
+            constexpr bool SM = decltype(SMc)::value;
+            unsigned long long m[3];
+#pragma unroll
+            for (int r = 0; r < 3; ++r) {
+                const float2 *row = bp + ra[r] + (SM ? d[r] : 0);
+                auto at = [&](int t) { return SM ? row[t] : __ldg(row + t); };
+                const int len = rl[r];
+                // 32-bit halves: cheaper bit operations than one 64-bit mask
+                unsigned lo = 0u, hi = 0u;
+                const int n0 = min(len, 32);
+#pragma unroll kViscUnroll
+                for (int t = 0; t < n0; ++t) {
+                    float2 e;
+                    const float r2 = dist2_packed(mp, at(t), e);
+                    // self and coincident particles are marked too; the
+                    // impulse skips them (r2 == 0)
+                    lo |= (unsigned)(r2 <= h2) << t;
+                }
+#pragma unroll kViscUnroll
+                for (int t = 32; t < len; ++t) {
+                    float2 e;
+                    const float r2 = dist2_packed(mp, at(t), e);
+                    hi |= (unsigned)(r2 <= h2) << (t - 32);
+                }
+                m[r] = ((unsigned long long)hi << 32) | lo;
+            }
+            m[1] &= ~(1ull << (i - ra[1]));  // self
+#pragma unroll
+            for (int r = 0; r < 3; ++r) {
+                const int dd = SM ? d[r] : 0;
+                walk_mask<float4>(
+                    m[r], ra[r], c.n,
+                    [&](int j) {
+                        if (SM) {
+                            const float2 q = bp[j + dd], w = bv[j + dd];
+                            return make_float4(q.x, q.y, w.x, w.y);
+                        }
+                        return load_pv(j);
+                    },
+                    [&](int, const float4 &dq) { impulse_core(dq, true); });
+            }
+        };
+        if (STAGED && staged)
+            two_phase(std::integral_constant<bool, true>(), sm_p, sm_v);
+        else
+            two_phase(std::integral_constant<bool, false>(), pos, vel);
+    } else if (search) {
+        for_each_candidate(key, start, g, capped, c.max_bucket, c.n, impulse);
     }
     if (PROBE) {
         probe_out[i] = dv;
@@ -731,6 +778,30 @@ __device__ __forceinline__ void viscosity_predict_one(
     kr_out[i] = make_uint2(k2, rank);
 }
 
+// The viscosity pass with the CTA's stencil rows (positions and velocities)
+// staged in shared memory.
+template <bool PERSIST>
+__global__ void __maxnreg__(48)
+k_viscosity_predict_sm(Ctx c, const DevState *__restrict__ st, const float2 *__restrict__ pos,
+                       const float2 *__restrict__ vel, const int *__restrict__ start,
+                       const unsigned *__restrict__ occ_in, unsigned *occ_reset,
+                       float2 *__restrict__ pos_out, float2 *__restrict__ prev_out,
+                       uint2 *__restrict__ kr_out, unsigned *__restrict__ cnt)
+{
+    extern __shared__ float2 sm_pv[];
+    pdl_enter();
+    if (blockIdx.x == 0 && threadIdx.x == 0) *occ_reset = 0u;
+    const bool capped = *occ_in > (unsigned)c.max_bucket;
+    const int cap = kStagePerThread * (int)blockDim.x;
+    const int ntiles = (c.n + blockDim.x - 1) / blockDim.x;
+    for (int tile = blockIdx.x; tile < ntiles; tile += PERSIST ? gridDim.x : ntiles) {
+        const int i = tile * blockDim.x + threadIdx.x;
+        viscosity_predict_one<false, true>(i, c, st, pos, vel, start, capped, pos_out, prev_out,
+                                           kr_out, cnt, nullptr, nullptr, i < c.n, sm_pv,
+                                           sm_pv + cap, cap);
+    }
+}
+
 // 48 registers: more resident warps than the compiler's free choice (55),
 // without spills.
 template <bool PROBE, bool PERSIST = false>
@@ -742,6 +813,7 @@ k_viscosity_predict(Ctx c, const DevState *__restrict__ st, const float2 *__rest
                     uint2 *__restrict__ kr_out, unsigned *__restrict__ cnt,
                     float2 *__restrict__ probe_out)
 {
+    pdl_enter();
     const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
     if (!PROBE && i0 == 0) *occ_reset = 0u;
     const bool capped = *occ_in > (unsigned)c.max_bucket;
@@ -882,6 +954,7 @@ k_density_sm(Ctx c, const float2 *__restrict__ pos, const int *__restrict__ star
              int4 *__restrict__ rows_out)
 {
     extern __shared__ float2 sm_pos[];
+    pdl_enter();
     const bool capped = *occ_in > (unsigned)c.max_bucket;
     const int ntiles = (c.n + blockDim.x - 1) / blockDim.x;
     for (int tile = blockIdx.x; tile < ntiles; tile += PERSIST ? gridDim.x : ntiles) {
@@ -900,6 +973,7 @@ k_density_t(Ctx c, const float2 *__restrict__ pos, const int *__restrict__ start
             ulonglong2 *__restrict__ mask01, unsigned long long *__restrict__ mask2,
             int4 *__restrict__ rows_out)
 {
+    pdl_enter();
     const bool capped = *occ_in > (unsigned)c.max_bucket;
     const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
     if (!PERSIST) {
@@ -953,6 +1027,40 @@ struct WalkConsts {
     float h_recip, kd, knd, hsd, hshd, Pd, Pnd;
 };
 
+// The scene's relaxation constants, and the walk's for particle record me =
+// (x, y, rho, rho_near): P = k (rho - rest), Pn = k_near rho_near
+// (fluid.c:563-564), pre-multiplied by dt^2.  One definition for every
+// relaxation path, so that their pair terms round identically.
+__device__ __forceinline__ RelaxConsts relax_consts(const Scene *__restrict__ S)
+{
+    RelaxConsts c;
+    c.hh = __ldg(&S->P.smoothing_radius);
+    c.h2 = __fmul_rn(c.hh, c.hh);
+    c.h_recip = __fdiv_rn(1.0f, c.hh);
+    const float dt = __ldg(&S->P.time_step);
+    c.dt2 = __fmul_rn(dt, dt);
+    c.k = __ldg(&S->P.k);
+    c.k_near = __ldg(&S->P.k_near);
+    c.rest = __ldg(&S->P.rest_density);
+    c.half_spring = __fmul_rn(0.5f, __ldg(&S->P.k_spring));
+    return c;
+}
+
+__device__ __forceinline__ WalkConsts walk_consts(const RelaxConsts &c, float4 me)
+{
+    const float Pi = __fmul_rn(c.k, __fsub_rn(me.z, c.rest));
+    const float Pni = __fmul_rn(c.k_near, me.w);
+    WalkConsts wc;
+    wc.h_recip = c.h_recip;
+    wc.kd = __fmul_rn(c.dt2, c.k);
+    wc.knd = __fmul_rn(c.dt2, c.k_near);
+    wc.hsd = __fmul_rn(c.dt2, c.half_spring);
+    wc.hshd = __fmul_rn(wc.hsd, c.hh);
+    wc.Pd = __fmul_rn(c.dt2, __fsub_rn(Pi, __fmul_rn(c.k, c.rest)));
+    wc.Pnd = __fmul_rn(c.dt2, Pni);
+    return wc;
+}
+
 __device__ __noinline__ bool owns_pair_of(const Scene *S, float2 p, const int *__restrict__ ids,
                                           int i, float2 q, int j)
 {
@@ -960,30 +1068,43 @@ __device__ __noinline__ bool owns_pair_of(const Scene *S, float2 p, const int *_
     return owns_pair(cell_key(p.x, p.y, g), ids[i], q, ids[j], g);
 }
 
-__device__ __forceinline__ void relax_pair_walk(const WalkConsts &c, float2 p, float4 q, int i,
+// The pair term of one neighbour (r2 <= h2 known): returns whether it
+// displaces the particle, by s (p - q) with d = q - p (the caller adds
+// -s d with one packed FMA), and counts a nudge of the pair's owner.
+__device__ __forceinline__ bool relax_pair_term(const WalkConsts &c, float2 p, float4 q, int i,
                                                 int j, const Scene *S,
-                                                const int *__restrict__ ids, float2 &a,
+                                                const int *__restrict__ ids, float &s, float2 &d,
                                                 int &nudges)
 {
-    float2 d;  // q - p: the negated pair offset, rounded as p - q is
+    // d = q - p: the negated pair offset, rounded as p - q is
     const float r2 = dist2_packed(make_float2(-p.x, -p.y), make_float2(q.x, q.y), d);
     if (r2 <= 2e-12f) {
         // r <= 1e-6 (rare): the owner of the pair is nudged (fluid.c:583-586)
         const float r = r2 > 0.0f ? __fsqrt_rn(r2) : 0.0f;
         if (j != i && r <= 0.000001f && owns_pair_of(S, p, ids, i, make_float2(q.x, q.y), j))
             ++nudges;
-        if (!(r > 0.0f)) return;
+        if (!(r > 0.0f)) return false;
     }
     const float r_recip = rsqrtf(r2);
     const float r = r2 * r_recip;
     const float ratio = r * c.h_recip;
-    if (ratio < 1.0f) {
-        const float omr = 1.0f - ratio;
-        const float D = (c.Pd + c.kd * q.z) * omr + (c.Pnd + c.knd * q.w) * omr * omr +
-                        (c.hshd - c.hsd * r);
-        const float s = D * r_recip;
+    if (!(ratio < 1.0f)) return false;
+    const float omr = 1.0f - ratio;
+    const float D = (c.Pd + c.kd * q.z) * omr + (c.Pnd + c.knd * q.w) * omr * omr +
+                    (c.hshd - c.hsd * r);
+    s = D * r_recip;
+    return true;
+}
+
+__device__ __forceinline__ void relax_pair_walk(const WalkConsts &c, float2 p, float4 q, int i,
+                                                int j, const Scene *S,
+                                                const int *__restrict__ ids, float2 &a,
+                                                int &nudges)
+{
+    float s;
+    float2 d;
+    if (relax_pair_term(c, p, q, i, j, S, ids, s, d, nudges))
         a = __ffma2_rn(make_float2(-s, -s), d, a);  // += s (p - q), per component
-    }
 }
 
 // double_density_relaxation (fluid.c:541-611) in gather form:
@@ -1017,6 +1138,40 @@ struct RowsIn {
     int d[3] = {0, 0, 0};
 };
 
+// The end of a particle's relaxation: x += the displacement and the owner's
+// nudges, boundaryConditions, then updateVelocity (fluid.c:627-653):
+// v = (x - x_prev)/dt clamped to +-5, and the new position's cell key
+// counted into the build of the relaxed positions.
+__device__ __forceinline__ void relax_finish(int i, const Ctx &cx, const Scene *S, float2 p,
+                                             float2 acc, int nudges,
+                                             const float2 *__restrict__ prev,
+                                             float2 *__restrict__ pos_out,
+                                             float2 *__restrict__ vel_out,
+                                             uint2 *__restrict__ kr_out,
+                                             unsigned *__restrict__ cnt, int *tile_made)
+{
+    const float nd = (float)nudges * 0.000001f;
+    float nx = __fadd_rn(__fadd_rn(p.x, acc.x), nd);
+    float ny = __fadd_rn(__fadd_rn(p.y, acc.y), nd);
+    boundary_of(nx, ny, S);
+    const float2 pv = prev[i];
+    const float dt_end = __ldg(&S->P.time_step);
+    const float vx = clamp5(__fdiv_rn(__fsub_rn(nx, pv.x), dt_end));
+    const float vy = clamp5(__fdiv_rn(__fsub_rn(ny, pv.y), dt_end));
+    const unsigned k2 = cell_key(nx, ny, load_grid(S));
+    unsigned rank = 0u;
+    if (in_bounds(k2, cx.M, kBadKey)) {
+        rank = atomicAdd(cnt + k2, 1u);
+        if (tile_made)
+            *tile_made = (int)(k2 / (unsigned)kBuildTile);
+        else
+            add_tile_count(cx.tile_cnt, k2);
+    }
+    pos_out[i] = make_float2(nx, ny);
+    vel_out[i] = make_float2(vx, vy);
+    kr_out[i] = make_uint2(k2, rank);
+}
+
 template <bool PROBE, bool LEARNED = false, bool LONG_ROWS = false>
 __device__ __forceinline__ void relax_update_one(
     int i, const Ctx &cx, const float4 *__restrict__ xr, const ulonglong2 *__restrict__ mask01,
@@ -1029,29 +1184,11 @@ __device__ __forceinline__ void relax_update_one(
 {
     const Scene *S = cx.scenes + scene_of(cx, i);
     const SG g = load_grid(S);
-    RelaxConsts c;
-    c.hh = __ldg(&S->P.smoothing_radius);
-    c.h2 = __fmul_rn(c.hh, c.hh);
-    c.h_recip = __fdiv_rn(1.0f, c.hh);
-    const float dt = __ldg(&S->P.time_step);
-    c.dt2 = dt * dt;
-    c.k = __ldg(&S->P.k);
-    c.k_near = __ldg(&S->P.k_near);
-    c.rest = __ldg(&S->P.rest_density);
-    c.half_spring = 0.5f * __ldg(&S->P.k_spring);
+    const RelaxConsts c = relax_consts(S);
 
     const float4 me = xr[i];
     const float2 p = make_float2(me.x, me.y);
-    const float Pi = c.k * (me.z - c.rest), Pni = c.k_near * me.w;
-    // constants of the masked walk, pre-multiplied by dt^2 (fewer live values)
-    WalkConsts wc;
-    wc.h_recip = c.h_recip;
-    wc.kd = c.dt2 * c.k;
-    wc.knd = c.dt2 * c.k_near;
-    wc.hsd = c.dt2 * c.half_spring;
-    wc.hshd = wc.hsd * c.hh;
-    wc.Pd = c.dt2 * (Pi - c.k * c.rest);
-    wc.Pnd = c.dt2 * Pni;
+    const WalkConsts wc = walk_consts(c, me);
     float2 acc = make_float2(0.0f, 0.0f);  // the displacement
     int nudges = 0;
     bool net = false;
@@ -1136,30 +1273,12 @@ __device__ __forceinline__ void relax_update_one(
             relax_pair_walk(wc, p, q, i, j, S, ids, acc, nudges);
         });
     }
-    const float nd = (float)nudges * 0.000001f;
     if (PROBE) {
+        const float nd = (float)nudges * 0.000001f;
         probe_out[i] = make_float2(acc.x + nd, acc.y + nd);
         return;
     }
-    float nx = __fadd_rn(__fadd_rn(p.x, acc.x), nd);
-    float ny = __fadd_rn(__fadd_rn(p.y, acc.y), nd);
-    boundary_of(nx, ny, S);
-    const float2 pv = prev[i];
-    const float dt_end = __ldg(&S->P.time_step);
-    const float vx = clamp5(__fdiv_rn(__fsub_rn(nx, pv.x), dt_end));
-    const float vy = clamp5(__fdiv_rn(__fsub_rn(ny, pv.y), dt_end));
-    const unsigned k2 = cell_key(nx, ny, load_grid(S));
-    unsigned rank = 0u;
-    if (in_bounds(k2, cx.M, kBadKey)) {
-        rank = atomicAdd(cnt + k2, 1u);
-        if (tile_made)
-            *tile_made = (int)(k2 / (unsigned)kBuildTile);
-        else
-            add_tile_count(cx.tile_cnt, k2);
-    }
-    pos_out[i] = make_float2(nx, ny);
-    vel_out[i] = make_float2(vx, vy);
-    kr_out[i] = make_uint2(k2, rank);
+    relax_finish(i, cx, S, p, acc, nudges, prev, pos_out, vel_out, kr_out, cnt, tile_made);
 }
 
 
@@ -1191,6 +1310,7 @@ k_relax_update_sm(Ctx c, const float4 *__restrict__ xr, const ulonglong2 *__rest
                   float2 *__restrict__ probe_out)
 {
     extern __shared__ float4 sm_rows[];
+    pdl_enter();
     if (!PROBE && blockIdx.x == 0 && threadIdx.x == 0) *occ_reset = 0u;
     const bool capped = *occ_in > (unsigned)c.max_bucket;
     const int ntiles = (c.n + blockDim.x - 1) / blockDim.x;
@@ -1222,6 +1342,7 @@ k_relax_update(Ctx c, const float4 *__restrict__ xr, const ulonglong2 *__restric
                uint2 *__restrict__ kr_out, unsigned *__restrict__ cnt,
                float2 *__restrict__ probe_out)
 {
+    pdl_enter();
     const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
     if (!PROBE && i0 == 0) *occ_reset = 0u;
     const bool capped = *occ_in > (unsigned)c.max_bucket;
@@ -1276,9 +1397,76 @@ k_relax_learned(Ctx c, const float4 *__restrict__ xr, const ulonglong2 *__restri
     }
 }
 
+// The plain relaxation and update of particle i by a whole warp: the lanes
+// test 32 stencil candidates at a time and evaluate the pair terms of the
+// hits in parallel; the displacement is then accumulated from them in slot
+// order, row by row, with the same packed FMA as the one-thread walk, so the
+// result is bit for bit the one-thread result (the plain step's).  Lane 0
+// finishes the particle.  The learned step's fallback particles are its
+// dense ones (long stencil rows): one thread each made them a long tail.
+__device__ __forceinline__ void relax_warp_one(
+    int i, const Ctx &cx, const float4 *__restrict__ xr, const ulonglong2 *__restrict__ mask01,
+    const unsigned long long *__restrict__ mask2, const int4 *__restrict__ rows,
+    const float2 *__restrict__ prev, const int *__restrict__ ids, const int *__restrict__ start,
+    bool capped, float2 *__restrict__ pos_out, float2 *__restrict__ vel_out,
+    uint2 *__restrict__ kr_out, unsigned *__restrict__ cnt)
+{
+    const unsigned lane = threadIdx.x & 31u;
+    if (capped) {
+        // overflowing buckets (pathological): the one-thread form
+        if (lane == 0)
+            relax_update_one<false, false, true>(i, cx, xr, mask01, mask2, rows, prev, ids, start,
+                                                 capped, pos_out, vel_out, kr_out, cnt, nullptr);
+        return;
+    }
+    const Scene *S = cx.scenes + scene_of(cx, i);
+    const SG g = load_grid(S);
+    const RelaxConsts c = relax_consts(S);
+    const float h2 = c.h2;
+    const float4 me = xr[i];
+    const float2 p = make_float2(me.x, me.y);
+    const WalkConsts wc = walk_consts(c, me);  // as relax_update_one's
+    float2 acc = make_float2(0.0f, 0.0f);
+    int nudges = 0;
+    const unsigned key = cell_key(p.x, p.y, g);
+    if (searchable(key, i, start, g, false, cx.max_bucket)) {
+        int ra[3], rl[3];
+        stencil_rows(key, start, g, ra, rl, cx.n);
+        const float2 mp = make_float2(-p.x, -p.y);
+        for (int r = 0; r < 3; ++r) {
+            for (int c0 = 0; c0 < rl[r]; c0 += 32) {
+                const int t = c0 + (int)lane;
+                const int j = ra[r] + t;
+                float s = 0.0f;
+                float2 d = make_float2(0.0f, 0.0f);
+                bool apply = false;
+                if (t < rl[r] && j != i && in_bounds(j, cx.n, kBadSlot)) {
+                    const float4 q = __ldg(xr + j);
+                    float2 e;
+                    if (dist2_packed(mp, make_float2(q.x, q.y), e) <= h2)
+                        apply = relax_pair_term(wc, p, q, i, j, S, ids, s, d, nudges);
+                }
+                unsigned hits = __ballot_sync(0xffffffffu, apply);
+                while (hits) {
+                    const int b = __ffs(hits) - 1;
+                    hits &= hits - 1u;
+                    const float sb = __shfl_sync(0xffffffffu, s, b);
+                    const float dx = __shfl_sync(0xffffffffu, d.x, b);
+                    const float dy = __shfl_sync(0xffffffffu, d.y, b);
+                    acc = __ffma2_rn(make_float2(-sb, -sb), make_float2(dx, dy), acc);
+                }
+            }
+        }
+        nudges = __reduce_add_sync(0xffffffffu, nudges);
+    }
+    if (lane == 0) relax_finish(i, cx, S, p, acc, nudges, prev, pos_out, vel_out, kr_out, cnt,
+                                nullptr);
+}
+
 // The fallback particles of a learned step: the plain relaxation + update
-// for each slot on fb_list (grid-stride: the count is known on the device
-// only).  Block 0 adds the count to the fallback statistics.
+// for each slot on fb_list, one warp per particle (grid-stride: the count is
+// known on the device only).  Block 0 adds the count to the fallback
+// statistics.
 __global__ void __launch_bounds__(kBlock, 4)
 k_relax_fallback(Ctx c, const float4 *__restrict__ xr, const ulonglong2 *__restrict__ mask01,
                  const unsigned long long *__restrict__ mask2, const int4 *__restrict__ rows,
@@ -1289,13 +1477,14 @@ k_relax_fallback(Ctx c, const float4 *__restrict__ xr, const ulonglong2 *__restr
                  unsigned *__restrict__ cnt, DevState *st, const int *__restrict__ fb_list)
 {
     const unsigned total = st->fb_count;
-    const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t0 == 0) atomicAdd(&st->learned_fallback, (unsigned long long)total);
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        atomicAdd(&st->learned_fallback, (unsigned long long)total);
     const bool capped = *occ_in > (unsigned)c.max_bucket;
-    for (unsigned k = t0; k < total; k += gridDim.x * blockDim.x)
-        relax_update_one<false, false, true>(fb_list[k], c, xr, mask01, mask2, rows, prev, ids,
-                                             start, capped, pos_out, vel_out, kr_out, cnt,
-                                             nullptr);
+    const unsigned w0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned nw = (gridDim.x * blockDim.x) >> 5;
+    for (unsigned k = w0; k < total; k += nw)
+        relax_warp_one(fb_list[k], c, xr, mask01, mask2, rows, prev, ids, start, capped, pos_out,
+                       vel_out, kr_out, cnt);
 }
 
 // ---------------------------------------------------------------------------
@@ -1493,6 +1682,31 @@ k_half_lists(Ctx c, const float2 *__restrict__ pos, const int *__restrict__ ids,
 
 static inline int blocks_for(int n, int bs = kBlock) { return (n + bs - 1) / bs; }
 
+// Launches one kernel of a step on the handle's stream.  With SPH_PDL it is
+// a programmatic dependent launch: the kernel may start launching while
+// its predecessor's last CTAs still run, and waits for the predecessor's
+// results in pdl_enter (in stream capture this becomes a programmatic edge
+// of the step's graph).
+#ifndef SPH_PDL
+#define SPH_PDL 1
+#endif
+template <typename... KArgs, typename... Args>
+static void launch_step(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                        cudaStream_t stream, Args &&...args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = SPH_PDL ? 1 : 0;
+    (void)cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+}
+
 // Grid of a gather launch for shape s.
 static inline dim3 gather_grid(const sph_cuda *h, const Shape &s)
 {
@@ -1531,9 +1745,9 @@ constexpr int kBuildPerThread = 2;
 
 static void enqueue_cell_starts(sph_cuda *h, int *out, unsigned *occ)
 {
-    k_cell_starts<<<build_tiles_of(h), kBuildThreads, 0, h->stream>>>(
-        h->cnt, h->M, h->d_nocell, h->build_tiles, out, h->d_state, occ, h->max_bucket,
-        h->max_neighbors);
+    launch_step(k_cell_starts, build_tiles_of(h), kBuildThreads, 0, h->stream, h->cnt, h->M,
+                (const unsigned *)h->d_nocell, (const unsigned *)h->build_tiles, out, h->d_state,
+                occ, h->max_bucket, h->max_neighbors);
 }
 
 static const char *const kKernelNames[] = {
@@ -1557,22 +1771,36 @@ static void enqueue_predict_sort(sph_cuda *h, Mark &mark)
     const Ctx c = make_ctx(h);
     DevState *st = h->d_state;
     {
+#if SPH_VISC_SMEM
+        auto kv = h->shape[0].persistent ? k_viscosity_predict_sm<true>
+                                         : k_viscosity_predict_sm<false>;
+        const size_t smem = 2 * (size_t)kStagePerThread * h->shape[0].block * sizeof(float2);
+        launch_step(kv, gather_grid(h, h->shape[0]), h->shape[0].block, smem, h->stream, c,
+                    (const DevState *)st, (const float2 *)h->pos_a, (const float2 *)h->vel_a,
+                    (const int *)h->start_a, (const unsigned *)&st->build_max_occ[SLOT_RELAXED],
+                    &st->build_max_occ[SLOT_PREDICTED], h->pos_b, h->prev_b, h->kr_b, h->cnt);
+#else
         auto kv = h->shape[0].persistent ? k_viscosity_predict<false, true>
                                          : k_viscosity_predict<false, false>;
-        kv<<<gather_grid(h, h->shape[0]), h->shape[0].block, 0, h->stream>>>(
-            c, st, h->pos_a, h->vel_a, h->start_a, &st->build_max_occ[SLOT_RELAXED],
-            &st->build_max_occ[SLOT_PREDICTED], h->pos_b, h->prev_b, h->kr_b, h->cnt, nullptr);
+        launch_step(kv, gather_grid(h, h->shape[0]), h->shape[0].block, 0, h->stream, c,
+                    (const DevState *)st, (const float2 *)h->pos_a, (const float2 *)h->vel_a,
+                    (const int *)h->start_a, (const unsigned *)&st->build_max_occ[SLOT_RELAXED],
+                    &st->build_max_occ[SLOT_PREDICTED], h->pos_b, h->prev_b, h->kr_b, h->cnt,
+                    (float2 *)nullptr);
+#endif
     }
     mark();
     enqueue_cell_starts(h, h->start_c, &st->build_max_occ[SLOT_PREDICTED]);
     mark();
     const int nbx = blocks_for(n, kBlock * kBuildPerThread);
-    k_scatter_ids_x<kBuildPerThread><<<nbx, kBlock, 0, h->stream>>>(
-        n, h->kr_b, h->id_a, h->start_c, h->tmp_id, h->build_tiles, build_tiles_of(h));
+    launch_step(k_scatter_ids_x<kBuildPerThread>, nbx, kBlock, 0, h->stream, n,
+                (const uint2 *)h->kr_b, (const int *)h->id_a, (const int *)h->start_c, h->tmp_id,
+                h->build_tiles, build_tiles_of(h));
     mark();
-    k_permute_x<kBuildPerThread><<<nbx, kBlock, 0, h->stream>>>(
-        n, h->kr_b, h->start_c, h->tmp_id, h->id_a, h->pos_b, h->prev_b, h->id_c, h->pos_c,
-        h->prev_c, nullptr);
+    launch_step(k_permute_x<kBuildPerThread>, nbx, kBlock, 0, h->stream, n,
+                (const uint2 *)h->kr_b, (const int *)h->start_c, (const int *)h->tmp_id,
+                (const int *)h->id_a, (const float2 *)h->pos_b, (const float2 *)h->prev_b,
+                h->id_c, h->pos_c, h->prev_c, (DevState *)nullptr);
     mark();
 }
 
@@ -1586,9 +1814,10 @@ static void enqueue_density(sph_cuda *h)
     auto kd = h->shape[1].persistent ? k_density_t<true> : k_density_t<false>;
     const size_t smem = 0;
 #endif
-    kd<<<gather_grid(h, h->shape[1]), h->shape[1].block, smem, h->stream>>>(
-        make_ctx(h), h->pos_c, h->start_c, &st->build_max_occ[SLOT_PREDICTED], h->xr_c,
-        h->mask01_c, h->mask2_c, h->rows_c);
+    launch_step(kd, gather_grid(h, h->shape[1]), h->shape[1].block, smem, h->stream, make_ctx(h),
+                (const float2 *)h->pos_c, (const int *)h->start_c,
+                (const unsigned *)&st->build_max_occ[SLOT_PREDICTED], h->xr_c, h->mask01_c,
+                h->mask2_c, h->rows_c);
 }
 
 // The C-order state of the next step's relaxation -- predicted positions,
@@ -1681,21 +1910,26 @@ int enqueue_step(sph_cuda *h, cudaEvent_t *events, int *nkernels, const tunable_
         auto kr = h->shape[2].persistent ? k_relax_update<false, true> : k_relax_update<false, false>;
         const size_t smem = 0;
 #endif
-        kr<<<gather_grid(h, h->shape[2]), h->shape[2].block, smem, h->stream>>>(
-            c, h->xr_c, h->mask01_c, h->mask2_c, h->rows_c, h->prev_c, h->id_c, h->start_c,
-            &st->build_max_occ[SLOT_PREDICTED], &st->build_max_occ[SLOT_RELAXED], h->pos_b,
-            h->vel_b, h->kr_b, h->cnt, nullptr);
+        launch_step(kr, gather_grid(h, h->shape[2]), h->shape[2].block, smem, h->stream, c,
+                    (const float4 *)h->xr_c, (const ulonglong2 *)h->mask01_c,
+                    (const unsigned long long *)h->mask2_c, (const int4 *)h->rows_c,
+                    (const float2 *)h->prev_c, (const int *)h->id_c, (const int *)h->start_c,
+                    (const unsigned *)&st->build_max_occ[SLOT_PREDICTED],
+                    &st->build_max_occ[SLOT_RELAXED], h->pos_b, h->vel_b, h->kr_b, h->cnt,
+                    (float2 *)nullptr);
         mark();
     }
     enqueue_cell_starts(h, h->start_a, &st->build_max_occ[SLOT_RELAXED]);
     mark();
     const int nbx = blocks_for(n, kBlock * kBuildPerThread);
-    k_scatter_ids_x<kBuildPerThread><<<nbx, kBlock, 0, h->stream>>>(
-        n, h->kr_b, h->id_c, h->start_a, h->tmp_id, h->build_tiles, build_tiles_of(h));
+    launch_step(k_scatter_ids_x<kBuildPerThread>, nbx, kBlock, 0, h->stream, n,
+                (const uint2 *)h->kr_b, (const int *)h->id_c, (const int *)h->start_a, h->tmp_id,
+                h->build_tiles, build_tiles_of(h));
     mark();
-    k_permute_x<kBuildPerThread><<<nbx, kBlock, 0, h->stream>>>(
-        n, h->kr_b, h->start_a, h->tmp_id, h->id_c, h->pos_b, h->vel_b, h->id_a, h->pos_a,
-        h->vel_a, st);
+    launch_step(k_permute_x<kBuildPerThread>, nbx, kBlock, 0, h->stream, n,
+                (const uint2 *)h->kr_b, (const int *)h->start_a, (const int *)h->tmp_id,
+                (const int *)h->id_c, (const float2 *)h->pos_b, (const float2 *)h->vel_b,
+                h->id_a, h->pos_a, h->vel_a, st);
     mark();
     if (nkernels) *nkernels = e - 1;
     return cuda_fail(cudaGetLastError(), "step launch");
