@@ -286,6 +286,28 @@ def traffic_per_launch(kernel: str, n: int):
         return None
 
 
+SMS, SCHEDULERS_PER_SM = 152, 4
+
+
+def issue_bound(kernel: str, n: int, kernel_ms: float, sm_mhz):
+    """The kernel's instruction-issue roofline: its warp instructions per
+    launch (a committed single-launch ncu capture, scaled by particles) over
+    its CUDA-event time, against one warp instruction per scheduler per
+    clock on every SM at the SM clock sampled during the run."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        d = json.load(open(p))
+        inst = d["kernels"][kernel]["warp_instructions"] * n / d["particles"]
+    except Exception:
+        return None
+    mhz = sm_mhz or 2070.0
+    achieved = inst / (kernel_ms / 1e3)
+    peak = SMS * SCHEDULERS_PER_SM * mhz * 1e6
+    return {"bound": "issue", "warp_instructions_per_launch": inst, "achieved": achieved,
+            "peak": peak, "unit": "warp instructions/s", "frac": achieved / peak,
+            "sm_mhz": mhz, "source": "profiles/traffic.json (ncu smsp__inst_executed.sum)"}
+
+
 class DamBreak:
     """The 4,194,304-particle dam break with the moving sphere mover."""
 
@@ -719,7 +741,8 @@ def run_gpu(args, world, rank):
                 "algorithmic_bytes_per_launch": alg,
                 "step_algorithmic_bytes": step_bytes,
                 "step_frac": step_bytes / (ms / K / 1e3) / 1e9 / peak,
-                "kernel_ms": {k: round(v, 5) for k, v in ktimes.items()}}
+                "kernel_ms": {k: round(v, 5) for k, v in ktimes.items()},
+                "issue": issue_bound(top, n, ktimes[top], clocks.get("sm_mhz"))}
 
     # ---- end to end through the C ABI with host buffers ----
     e2e = None

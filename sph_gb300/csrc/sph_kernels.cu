@@ -966,8 +966,11 @@ k_density_sm(Ctx c, const float2 *__restrict__ pos, const int *__restrict__ star
 
 // 32 registers (four 512-thread CTAs' worth per SM): full occupancy for this
 // issue-bound pass outweighs the few spilled values of its rare paths.
+#ifndef SPH_DENS_MIN_BLOCKS
+#define SPH_DENS_MIN_BLOCKS 4  // resident 512-thread CTAs per SM the density pass is built for
+#endif
 template <bool PERSIST>
-__global__ void __launch_bounds__(kMaxBlock, 4)
+__global__ void __launch_bounds__(kMaxBlock, SPH_DENS_MIN_BLOCKS)
 k_density_t(Ctx c, const float2 *__restrict__ pos, const int *__restrict__ start,
             const unsigned *__restrict__ occ_in, float4 *__restrict__ xr_out,
             ulonglong2 *__restrict__ mask01, unsigned long long *__restrict__ mask2,
