@@ -55,9 +55,10 @@ struct DevState {
     unsigned int list_cap_risk;
     unsigned int lists_valid;      // a neighbour relation exists: viscosity is on
     unsigned int build_max_occ[4]; // per build slot, reset by the build's key producer
-    unsigned int fb_count;         // learned step: particles on the fallback list
+    unsigned int fb_count;         // learned step: fallback particles with masked rows (list front)
+    unsigned int fb_long;          // ... and with rows too long for a mask (list back)
     unsigned int tile_count_mismatch;  // a build's tile counts disagreed with its counters
-    unsigned int pad[3];
+    unsigned int pad[2];
     unsigned long long learned_steps;     // steps run with a learned model attached
     unsigned long long learned_fallback;  // particle-steps of those that used the plain relaxation
 };

@@ -1390,13 +1390,26 @@ k_relax_learned(Ctx c, const float4 *__restrict__ xr, const ulonglong2 *__restri
                                       vel_out, kr_out, cnt, probe_out, L, &used, &t);
     if (PROBE) return;
     if (c.tile_cnt) cta_tile_count(c.tile_cnt, t);
-    const unsigned fb = __ballot_sync(0xffffffffu, !used);
-    if (fb) {
-        const int lane = threadIdx.x & 31, leader = __ffs(fb) - 1;
+    // fallback particles: those whose stencil rows fit the hit masks go to
+    // the front of fb_list (one thread each in k_relax_fallback), those with
+    // a row too long for a mask to the back (one warp each)
+    const bool longrow = !used && __ldg(rows + i).w == kRowsFull;
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned fbs = __ballot_sync(0xffffffffu, !used && !longrow);
+    const unsigned fbl = __ballot_sync(0xffffffffu, longrow);
+    if (fbs) {
+        const int leader = __ffs(fbs) - 1;
         unsigned base = 0;
-        if (lane == leader) base = atomicAdd(&st->fb_count, (unsigned)__popc(fb));
+        if (lane == (unsigned)leader) base = atomicAdd(&st->fb_count, (unsigned)__popc(fbs));
         base = __shfl_sync(0xffffffffu, base, leader);
-        if (!used) fb_list[base + __popc(fb & ((1u << lane) - 1u))] = i;
+        if (!used && !longrow) fb_list[base + __popc(fbs & ((1u << lane) - 1u))] = i;
+    }
+    if (fbl) {
+        const int leader = __ffs(fbl) - 1;
+        unsigned base = 0;
+        if (lane == (unsigned)leader) base = atomicAdd(&st->fb_long, (unsigned)__popc(fbl));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (longrow) fb_list[c.n - 1 - (int)(base + __popc(fbl & ((1u << lane) - 1u)))] = i;
     }
 }
 
@@ -1467,9 +1480,11 @@ __device__ __forceinline__ void relax_warp_one(
 }
 
 // The fallback particles of a learned step: the plain relaxation + update
-// for each slot on fb_list, one warp per particle (grid-stride: the count is
-// known on the device only).  Block 0 adds the count to the fallback
-// statistics.
+// for each slot on fb_list -- one thread per particle for those at its front
+// (rows within the hit masks), then one warp per particle for those at its
+// back (a row too long for a mask: the densest, whose one-thread walks were
+// the long tail).  Grid-stride loops: the counts are known on the device
+// only.  Block 0 adds the counts to the fallback statistics.
 __global__ void __launch_bounds__(kBlock, 4)
 k_relax_fallback(Ctx c, const float4 *__restrict__ xr, const ulonglong2 *__restrict__ mask01,
                  const unsigned long long *__restrict__ mask2, const int4 *__restrict__ rows,
@@ -1479,15 +1494,31 @@ k_relax_fallback(Ctx c, const float4 *__restrict__ xr, const ulonglong2 *__restr
                  float2 *__restrict__ vel_out, uint2 *__restrict__ kr_out,
                  unsigned *__restrict__ cnt, DevState *st, const int *__restrict__ fb_list)
 {
-    const unsigned total = st->fb_count;
+    const unsigned total = st->fb_count, total_long = st->fb_long;
     if (blockIdx.x == 0 && threadIdx.x == 0)
-        atomicAdd(&st->learned_fallback, (unsigned long long)total);
+        atomicAdd(&st->learned_fallback, (unsigned long long)(total + total_long));
     const bool capped = *occ_in > (unsigned)c.max_bucket;
-    const unsigned w0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const unsigned nw = (gridDim.x * blockDim.x) >> 5;
-    for (unsigned k = w0; k < total; k += nw)
-        relax_warp_one(fb_list[k], c, xr, mask01, mask2, rows, prev, ids, start, capped, pos_out,
-                       vel_out, kr_out, cnt);
+    const unsigned t0 = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned nt = gridDim.x * blockDim.x;
+    for (unsigned k = t0; k < total; k += nt)
+        relax_update_one<false, false, true>(fb_list[k], c, xr, mask01, mask2, rows, prev, ids,
+                                             start, capped, pos_out, vel_out, kr_out, cnt,
+                                             nullptr);
+    // the long-row particles: a warp each when they are few enough for one
+    // pass of the grid's warps (the long tail of a step with a few dense
+    // spots), else a thread each (many dense particles: a warp each would
+    // leave most of them waiting).  Both sum in slot order: the same bits.
+    const unsigned w0 = t0 >> 5, nw = nt >> 5;
+    if (total_long <= nw) {
+        for (unsigned k = w0; k < total_long; k += nw)
+            relax_warp_one(fb_list[c.n - 1 - (int)k], c, xr, mask01, mask2, rows, prev, ids,
+                           start, capped, pos_out, vel_out, kr_out, cnt);
+    } else {
+        for (unsigned k = t0; k < total_long; k += nt)
+            relax_update_one<false, false, true>(fb_list[c.n - 1 - (int)k], c, xr, mask01, mask2,
+                                                 rows, prev, ids, start, capped, pos_out, vel_out,
+                                                 kr_out, cnt, nullptr);
+    }
 }
 
 // ---------------------------------------------------------------------------

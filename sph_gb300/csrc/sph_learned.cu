@@ -90,7 +90,10 @@ k_features(Ctx c, const float2 *__restrict__ pos, const float2 *__restrict__ pre
            unsigned short *__restrict__ nbcount, unsigned *__restrict__ fb_count)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i == 0 && fb_count) *fb_count = 0u;
+    if (i == 0 && fb_count) {  // both fallback counters of the step (fb_count, fb_long)
+        fb_count[0] = 0u;
+        fb_count[1] = 0u;
+    }
     if (i >= c.n) return;
     const Scene *S = c.scenes + scene_of(c, i);
     const SG g = load_grid(S);
