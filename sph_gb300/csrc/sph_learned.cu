@@ -24,6 +24,7 @@
 #include "sph_learned.h"
 #include "sph_tc.cuh"
 
+
 namespace sph {
 
 int launch_probe(sph_cuda *h, int which, void *scratch, float2 *out);
@@ -176,6 +177,8 @@ k_features(Ctx c, const float2 *__restrict__ pos, const float2 *__restrict__ pre
                 for (int r = 0; r < 3; ++r)
                     walk_mask<float2>(m[r], ra[r], c.n, [&](int j) { return __ldg(pos + j); }, visit);
             } else {
+                // a row longer than one mask (dense cells): one pass, the
+                // terms of each hit as the filter finds it, in slot order
 #pragma unroll
                 for (int r = 0; r < 3; ++r) {
                     const float2 *row = pos + ra[r];

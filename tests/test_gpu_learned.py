@@ -72,8 +72,8 @@ def test_mlp_forward_matches_numpy(cuda_lib):
         # tanh.approx against tanh: an occasional BF16 ulp in an activation
         # (any layout or indexing fault gives errors of the order of the outputs)
         d = y[:, :3] - ref[:, :3]
-        assert np.abs(d).max() <= 3e-2 * np.abs(ref[:, :3]).max(), np.abs(d).max()
-        assert np.sqrt(np.mean(d ** 2)) <= 1.5e-2 * np.sqrt(np.mean(ref[:, :3] ** 2))
+        assert np.abs(d).max() <= 1.5e-2 * np.abs(ref[:, :3]).max(), np.abs(d).max()
+        assert np.sqrt(np.mean(d ** 2)) <= 1e-2 * np.sqrt(np.mean(ref[:, :3] ** 2))
         assert np.all(y[:, 3:] == 0.0)
         # rows are independent: a prefix gives the same rows
         assert np.array_equal(m.forward(x[:130]), y[:130])
