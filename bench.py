@@ -340,6 +340,8 @@ class DamBreak:
     def advance(self, sim, t0, k):
         sim.step_schedule([self.p(t) for t in range(t0, t0 + k)])
 
+    tunables_bytes = 64  # one tunable_parameters record per step (fluid.h:78-97)
+
     def step_one(self, sim, t):
         sim.step(self.p(t))
 
@@ -377,6 +379,8 @@ class EnsembleWork:
 
     def advance(self, sim, t0, k):
         sim.step(None, k)
+
+    tunables_bytes = 0  # the scenes keep their tunables
 
     def step_one(self, sim, t):
         sim.step(None, 1)
@@ -788,11 +792,13 @@ def run_gpu(args, world, rank):
         sim2.wait_coords(coords[(W + K - 1) % 2].array)
         t_e2e = time.perf_counter() - tw
         sim2.close()
+        state_bytes = sum(pa.array.nbytes for pa in staged)
         for c in coords + staged:
             c.free()
         t_e2e = max_over_ranks(world, t_e2e)
         e2e = {"value": world * n * (W + K) / t_e2e, "unit": "particle-steps/s",
-               "h2d_bytes_per_step": int(64 + 32 * n / (W + K)), "d2h_bytes_per_step": 4 * n,
+               "h2d_bytes_per_step": int(work.tunables_bytes + state_bytes / (W + K)),
+               "d2h_bytes_per_step": 4 * n,
                "steps": W + K, "includes": "state upload from page-locked host memory, then per "
                                            "step the tunables H2D, the full step and the packed "
                                            "coordinates D2H (pinned, double-buffered: frame t's "

@@ -222,7 +222,9 @@ int sph_cuda_pack_coords_short(sph_cuda_t *h, short *coords, int n);
  * next sph_cuda_step; sph_cuda_coords_wait(h, coords) returns once they
  * have arrived.  Two copies may be in flight (alternate two buffers, as the
  * reference overlaps its MPI_Isend with the next steps, fluid.c:282-287,
- * 356-364); a third call waits for the oldest. */
+ * 356-364); a third call waits for the oldest.  The two device staging
+ * buffers and the copy stream are made with the handle: the call allocates
+ * nothing. */
 int sph_cuda_pack_coords_async(sph_cuda_t *h, short *coords, int n);
 int sph_cuda_coords_wait(sph_cuda_t *h, const short *coords);
 

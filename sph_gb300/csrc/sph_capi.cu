@@ -270,6 +270,37 @@ static int push_scenes(sph_cuda *h)
 }
 
 // Allocates a handle for `scenes` (cell offsets filled in here).
+// The coordinate frames' resources: two device staging buffers of
+// capacity + 1 packed coordinates, their pack and copy events, and the copy
+// stream.  Made with the handle (so a frame loop allocates nothing), all or
+// nothing.
+static int ensure_frames(sph_cuda *h)
+{
+    if (h->copy_stream) return SPH_OK;
+    auto undo = [&]() {
+        for (int k = 0; k < 2; ++k) {
+            if (h->d_coords[k]) cudaFree(h->d_coords[k]);
+            if (h->pack_ev[k]) cudaEventDestroy(h->pack_ev[k]);
+            if (h->copy_ev[k]) cudaEventDestroy(h->copy_ev[k]);
+            h->d_coords[k] = nullptr;
+            h->pack_ev[k] = h->copy_ev[k] = nullptr;
+        }
+    };
+    int rc = SPH_OK;
+    for (int k = 0; k < 2 && !rc; ++k) {
+        rc = cuda_fail(device_alloc((void **)&h->d_coords[k],
+                                    ((size_t)h->capacity + 1) * sizeof(short2)), "cudaMalloc");
+        if (!rc) rc = cuda_fail(cudaEventCreateWithFlags(&h->pack_ev[k], cudaEventDisableTiming),
+                                "cudaEventCreate");
+        if (!rc) rc = cuda_fail(cudaEventCreateWithFlags(&h->copy_ev[k], cudaEventDisableTiming),
+                                "cudaEventCreate");
+    }
+    if (!rc) rc = cuda_fail(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking),
+                            "cudaStreamCreate");
+    if (rc) undo();
+    return rc;
+}
+
 static int build_handle(sph_cuda **out, std::vector<Scene> &&scenes, int capacity, int max_bucket,
                         int max_neighbors)
 {
@@ -367,6 +398,7 @@ static int build_handle(sph_cuda **out, std::vector<Scene> &&scenes, int capacit
         if (rc) return fail(rc);
     }
     rc = push_scenes(h);
+    if (!rc) rc = ensure_frames(h);
     if (rc) return fail(rc);
     *out = h;
     return SPH_OK;
@@ -763,33 +795,7 @@ int sph_cuda_pack_coords_async(sph_cuda_t *h, short *coords, int n)
         set_error("pack: n %d (handle holds %d) or null buffer", n, h->n);
         return SPH_ERR_INVALID;
     }
-    if (!h->copy_stream) {
-        // all or nothing: a failed set-up leaves no half-made resources
-        auto undo = [&]() {
-            for (int k = 0; k < 2; ++k) {
-                if (h->d_coords[k]) cudaFree(h->d_coords[k]);
-                if (h->pack_ev[k]) cudaEventDestroy(h->pack_ev[k]);
-                if (h->copy_ev[k]) cudaEventDestroy(h->copy_ev[k]);
-                h->d_coords[k] = nullptr;
-                h->pack_ev[k] = h->copy_ev[k] = nullptr;
-            }
-        };
-        int rc = SPH_OK;
-        for (int k = 0; k < 2 && !rc; ++k) {
-            rc = cuda_fail(device_alloc((void **)&h->d_coords[k],
-                                        ((size_t)h->capacity + 1) * sizeof(short2)), "cudaMalloc");
-            if (!rc) rc = cuda_fail(cudaEventCreateWithFlags(&h->pack_ev[k], cudaEventDisableTiming),
-                                    "cudaEventCreate");
-            if (!rc) rc = cuda_fail(cudaEventCreateWithFlags(&h->copy_ev[k], cudaEventDisableTiming),
-                                    "cudaEventCreate");
-        }
-        if (!rc) rc = cuda_fail(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking),
-                                "cudaStreamCreate");
-        if (rc) {
-            undo();
-            return rc;
-        }
-    }
+    SPH_TRY(ensure_frames(h));
     const int k = h->pack_slot;
     // the copy made from this staging buffer two calls ago must be complete
     if (h->copy_dst[k]) SPH_CUDA(cudaEventSynchronize(h->copy_ev[k]));

@@ -49,6 +49,15 @@
 #ifndef SPH_VISC_SMEM
 #define SPH_VISC_SMEM 0   // viscosity pass likewise
 #endif
+// The density filter computes every candidate's terms and adds those of
+// the hits (no branch per candidate; the sums are bit-identical).
+#ifndef SPH_DENS_BRANCHFREE
+#define SPH_DENS_BRANCHFREE 0
+#endif
+// The relaxation's masked walk keeps two neighbour loads in flight.
+#ifndef SPH_RELAX_WALK2
+#define SPH_RELAX_WALK2 0
+#endif
 
 namespace sph {
 // Shared-memory elements a gather CTA stages per thread of the CTA (the
@@ -863,7 +872,11 @@ __device__ __forceinline__ void density_filter(int i, float2 mp, float h2, float
             for (int t = 32 * hh; t < t1; ++t) {
                 float2 e;
                 const float r2 = dist2_packed(mp, at(t), e);
-                if (r2 <= h2 && (r != 1 || t != self)) {
+                const bool hit = r2 <= h2 && (r != 1 || t != self);
+                if (SPH_DENS_BRANCHFREE) {
+                    mh[hh] |= (unsigned)hit << (t & 31);
+                    add_density_if(ab, r2, h_recip, hit);
+                } else if (hit) {
                     mh[hh] |= 1u << (t & 31);
                     add_density(ab, r2, h_recip);
                 }
@@ -1259,6 +1272,14 @@ __device__ __forceinline__ void relax_update_one(
                         relax_pair_walk(wc, p, q, i, j, S, ids, acc, nudges);
                     });
             }
+        } else if (SPH_RELAX_WALK2) {
+#pragma unroll
+            for (int r = 0; r < 3; ++r)
+                walk_mask2<float4>(
+                    mm[r], ra[r], cx.n, [&](int j) { return __ldg(xr + j); },
+                    [&](int j, const float4 &q) {
+                        relax_pair_walk(wc, p, q, i, j, S, ids, acc, nudges);
+                    });
         } else {
 #pragma unroll
             for (int r = 0; r < 3; ++r)
