@@ -174,17 +174,6 @@ __device__ __forceinline__ void add_density(float2 &ab, float r2, float h_recip)
     }
 }
 
-// add_density for a candidate that may not be a neighbour: the terms are
-// computed either way and a non-neighbour adds (+0, +0), which leaves the
-// sums' bits as they are.
-__device__ __forceinline__ void add_density_if(float2 &ab, float r2, float h_recip, bool hit)
-{
-    const float ratio = __fmul_rn(__fsqrt_rn(r2), h_recip);
-    const float omr = (hit && ratio < 1.0f) ? __fsub_rn(1.0f, ratio) : 0.0f;
-    const float omr2 = __fmul_rn(omr, omr);
-    ab = __fadd2_rn(ab, make_float2(omr2, __fmul_rn(omr2, omr)));
-}
-
 // dist2 of p and q in packed FP32x2 arithmetic (sm_100+): d = q - p per
 // component (given mp = -p), r2 = d.x^2 + d.y^2, each operation rounded
 // exactly as dist2(p.x - q.x, p.y - q.y) rounds it (the squares of +-dx
@@ -424,45 +413,6 @@ __device__ __forceinline__ void walk_mask(unsigned long long m, int base, int n,
         }
     }
     if (have) visit(jp, dp);
-}
-
-// walk_mask with two neighbours' loads in flight ahead of the visit (same
-// visit order, so the same sums): for a walk whose visits are short next to
-// a load's latency.
-template <class T, class Load, class Visit>
-__device__ __forceinline__ void walk_mask2(unsigned long long m, int base, int n, Load load,
-                                           Visit visit)
-{
-    unsigned half[2] = {(unsigned)m, (unsigned)(m >> 32)};
-    int held = 0;  // loads in flight: a (older), b
-    int ja = 0, jb = 0;
-    T da{}, db{};
-#pragma unroll
-    for (int hh = 0; hh < 2; ++hh) {
-        unsigned b = half[hh];
-        while (b) {
-            const int j = base + 32 * hh + __ffs(b) - 1;
-            b &= b - 1u;
-            if (!in_bounds(j, n, kBadSlot)) continue;
-            const T d = load(j);
-            if (held == 2) {
-                visit(ja, da);
-                ja = jb;
-                da = db;
-            } else {
-                ++held;
-            }
-            if (held == 1) {
-                ja = j;
-                da = d;
-            } else {
-                jb = j;
-                db = d;
-            }
-        }
-    }
-    if (held >= 1) visit(ja, da);
-    if (held == 2) visit(jb, db);
 }
 
 // The neighbours (r2 <= h2, r2 exact as dist2_packed rounds it) of one

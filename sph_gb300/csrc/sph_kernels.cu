@@ -49,15 +49,6 @@
 #ifndef SPH_VISC_SMEM
 #define SPH_VISC_SMEM 0   // viscosity pass likewise
 #endif
-// The density filter computes every candidate's terms and adds those of
-// the hits (no branch per candidate; the sums are bit-identical).
-#ifndef SPH_DENS_BRANCHFREE
-#define SPH_DENS_BRANCHFREE 0
-#endif
-// The relaxation's masked walk keeps two neighbour loads in flight.
-#ifndef SPH_RELAX_WALK2
-#define SPH_RELAX_WALK2 0
-#endif
 
 namespace sph {
 // Shared-memory elements a gather CTA stages per thread of the CTA (the
@@ -872,11 +863,7 @@ __device__ __forceinline__ void density_filter(int i, float2 mp, float h2, float
             for (int t = 32 * hh; t < t1; ++t) {
                 float2 e;
                 const float r2 = dist2_packed(mp, at(t), e);
-                const bool hit = r2 <= h2 && (r != 1 || t != self);
-                if (SPH_DENS_BRANCHFREE) {
-                    mh[hh] |= (unsigned)hit << (t & 31);
-                    add_density_if(ab, r2, h_recip, hit);
-                } else if (hit) {
+                if (r2 <= h2 && (r != 1 || t != self)) {
                     mh[hh] |= 1u << (t & 31);
                     add_density(ab, r2, h_recip);
                 }
@@ -1203,6 +1190,19 @@ __device__ __forceinline__ void relax_update_one(
     const RelaxConsts c = relax_consts(S);
 
     const float4 me = xr[i];
+    // the plain pass requests the hit masks with the record and prefetches
+    // the previous position, so that their DRAM latencies overlap instead of
+    // following one another (the record decides whether the masks are used;
+    // relax_finish reads the previous position): 7% off this latency-bound
+    // pass
+    constexpr bool kHoist = !LEARNED;
+    ulonglong2 m01h = make_ulonglong2(0ull, 0ull);
+    unsigned long long m2h = 0ull;
+    if (kHoist && rows) {
+        m01h = __ldg(mask01 + i);
+        m2h = __ldg(mask2 + i);
+        asm volatile("prefetch.global.L1 [%0];" ::"l"(prev + i));
+    }
     const float2 p = make_float2(me.x, me.y);
     const WalkConsts wc = walk_consts(c, me);
     float2 acc = make_float2(0.0f, 0.0f);  // the displacement
@@ -1260,8 +1260,8 @@ __device__ __forceinline__ void relax_update_one(
         }
     }
     if (mode == kRowsMasked) {
-        const ulonglong2 m01 = mask01[i];
-        const unsigned long long mm[3] = {m01.x, m01.y, mask2[i]};
+        const ulonglong2 m01 = kHoist ? m01h : mask01[i];
+        const unsigned long long mm[3] = {m01.x, m01.y, kHoist ? m2h : mask2[i]};
         if (R.sm) {
 #pragma unroll
             for (int r = 0; r < 3; ++r) {
@@ -1272,14 +1272,6 @@ __device__ __forceinline__ void relax_update_one(
                         relax_pair_walk(wc, p, q, i, j, S, ids, acc, nudges);
                     });
             }
-        } else if (SPH_RELAX_WALK2) {
-#pragma unroll
-            for (int r = 0; r < 3; ++r)
-                walk_mask2<float4>(
-                    mm[r], ra[r], cx.n, [&](int j) { return __ldg(xr + j); },
-                    [&](int j, const float4 &q) {
-                        relax_pair_walk(wc, p, q, i, j, S, ids, acc, nudges);
-                    });
         } else {
 #pragma unroll
             for (int r = 0; r < 3; ++r)
