@@ -125,7 +125,8 @@ k_features(Ctx c, const float2 *__restrict__ pos, const float2 *__restrict__ pre
             // one neighbour's terms (never the particle itself): density
             // (add_density's rounding, so that the records equal the plain
             // density pass's bit for bit), messages, counts
-            auto visit = [&](int j, const float2 &q) {
+            // qp: the neighbour's previous position
+            auto visit_p = [&](int j, const float2 &q, const float2 &qp) {
                 float2 e;  // q - p
                 const float r2 = dist2_packed(mp, q, e);
                 const float rinv = rsqrtf(r2);
@@ -146,10 +147,10 @@ k_features(Ctx c, const float2 *__restrict__ pos, const float2 *__restrict__ pre
                     Tdiag = __ffma2_rn(wu, u, Tdiag);
                     Txy += wu.x * u.y;
                     // sum w (x_j - x_prev_j); the velocities follow at the end
-                    const float2 qp = __ldg(prev + j);
                     Dsum = __ffma2_rn(w2, __fadd2_rn(q, make_float2(-qp.x, -qp.y)), Dsum);
                 }
             };
+            auto visit = [&](int j, const float2 &q) { visit_p(j, q, __ldg(prev + j)); };
             const int self = i - ra[1];  // the particle's own slot in row 1
             if (rl[0] <= kMaskRow && rl[1] <= kMaskRow && rl[2] <= kMaskRow) {
                 rec = make_int4(ra[0], ra[1], ra[2], kRowsMasked);
@@ -173,9 +174,19 @@ k_features(Ctx c, const float2 *__restrict__ pos, const float2 *__restrict__ pre
                     m[r] = ((unsigned long long)hi << 32) | lo;
                 }
                 m[1] &= ~(1ull << self);
+                // the walk loads each hit's position and previous position
+                // together, one hit ahead of its terms
 #pragma unroll
                 for (int r = 0; r < 3; ++r)
-                    walk_mask<float2>(m[r], ra[r], c.n, [&](int j) { return __ldg(pos + j); }, visit);
+                    walk_mask<float4>(
+                        m[r], ra[r], c.n,
+                        [&](int j) {
+                            const float2 q = __ldg(pos + j), qp = __ldg(prev + j);
+                            return make_float4(q.x, q.y, qp.x, qp.y);
+                        },
+                        [&](int j, const float4 &d) {
+                            visit_p(j, make_float2(d.x, d.y), make_float2(d.z, d.w));
+                        });
             } else {
                 // a row longer than one mask (dense cells): one pass, the
                 // terms of each hit as the filter finds it, in slot order
