@@ -442,12 +442,14 @@ k_mlp(int n, const __nv_bfloat16 *__restrict__ feat, const __nv_bfloat16 *__rest
             tc::mma_tile(tacc, sx, tc::smem_u32(S.w.w1), HID, IN, false);
             tc::mma_commit(&P.mbar);
         }
+        // the next tile's features, loaded now and stored at the end of this
+        // tile: their DRAM latency hides behind the whole tile, not behind
+        // layer 1 alone (6% off the kernel)
         uint4 na, nb;
         load_feat(feat, n, tile + stride, tp, na, nb);
         bool done = tc::mbar_wait(&P.mbar, phase);
         phase ^= 1u;
         tc::fence_after_sync();
-        store_feat(P.x, tp, na, nb);  // layer 1 has consumed x
         hidden_epilogue(P.hbuf, tacc, tp);
         tc::fence_async_smem();
         tc::fence_before_sync();
@@ -486,6 +488,8 @@ k_mlp(int n, const __nv_bfloat16 *__restrict__ feat, const __nv_bfloat16 *__rest
             if (gi < n && done)
                 __stcs(out + gi, make_float4(v[0] + S.w.b3[0], v[1] + S.w.b3[1], v[2] + S.w.b3[2], 0.0f));
         }
+        store_feat(P.x, tp, na, nb);  // layer 1 consumed x long ago
+        tc::fence_async_smem();
         tc::fence_before_sync();
         ok = tc::named_sync_and(bar, kPipeThreads, done);  // read before layer 1 reuses it
         tc::fence_after_sync();
