@@ -6,9 +6,11 @@
  *
  * Model.  A message-passing network over each particle's neighbours within h
  * (particles with more than 48 take the plain relaxation): messages are the
- * neighbour offsets and relative velocities, weighted by (1 - r/h)^p and
- * aggregated into a 32-wide feature row, joined with the particle's own
- * density and near density and its scene's stiffness ratios; a 2-layer
+ * neighbour offsets, relative velocities, densities and near densities,
+ * weighted by (1 - r/h)^p and aggregated into a 32-wide feature row, joined
+ * with the particle's own density and near density and its scene's
+ * stiffness ratios (the step's density pass computes every density first,
+ * then a walk of its hit masks gathers the messages); a 2-layer
  * width-128 GELU MLP
  * maps the row to the relaxation displacement (in units of
  * s = h dt^2 (k + k_near + k_spring)) and to a predicted density error.

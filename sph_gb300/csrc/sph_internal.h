@@ -204,6 +204,7 @@ int enqueue_step(sph_cuda *h, cudaEvent_t *events, int *nkernels,
 unsigned bounds_flags_kernels();  // checked builds (SPH_BOUNDS_CHECK): recorded index faults
 unsigned bounds_flags_learned();
 int enqueue_predicted_state(sph_cuda *h);       // first half of a step: C order + density
+int launch_density_pass(sph_cuda *h);            // the density pass on the C order
 int launch_learned_passes(sph_cuda *h, cudaEvent_t *events);  // features + network (C order)
 int launch_learned_relax(sph_cuda *h, float2 *probe_out, cudaEvent_t *events = nullptr);
 void free_learned_buffers(sph_cuda *h);

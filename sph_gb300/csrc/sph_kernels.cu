@@ -1871,6 +1871,14 @@ static void enqueue_density(sph_cuda *h)
                 h->mask2_c, h->rows_c);
 }
 
+// The density pass of a step (the learned step's features start with it).
+int launch_density_pass(sph_cuda *h)
+{
+    if (h->n == 0) return SPH_OK;
+    enqueue_density(h);
+    return cuda_fail(cudaGetLastError(), "density");
+}
+
 // The C-order state of the next step's relaxation -- predicted positions,
 // their cell starts, density records and hit masks -- without advancing:
 // the A state is left as it is (the last step's density record in xr_c is

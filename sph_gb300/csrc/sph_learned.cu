@@ -1,8 +1,9 @@
 // sph_learned.cu -- learned relaxation (include/sph_learned.h).
 //
-//   k_features   density pass + neighbour message aggregation -> 32-wide BF16
-//                feature rows and neighbour counts (replaces k_density in a
-//                learned step; writes the same density records and masks)
+//   k_messages   after the plain density pass: a walk of its hit masks that
+//                aggregates the neighbour messages (offsets, velocities,
+//                densities and near densities) -> 32-wide BF16 feature rows
+//                and neighbour counts
 //   k_mlp        fused 2-layer width-128 GELU MLP on the tcgen05 tensor cores:
 //                one CTA per SM of four 256-thread pipelines, weights
 //                resident in shared memory, FP32 accumulators in tensor memory
@@ -64,30 +65,36 @@ __device__ __forceinline__ float out_scale(const Scene *__restrict__ S)
 }
 
 // ---------------------------------------------------------------------------
-// feature pass
+// message pass
 // ---------------------------------------------------------------------------
 
-// Density and near density exactly as the plain density pass computes them
-// (same records, same hit masks, same summation order), plus the particle's
-// feature row.  Messages of the neighbours j with r/h < 1 (self excluded),
+// A neighbour's record for the message walk: (x, y, rho, rho_near) and its
+// previous position.
+struct NbRec {
+    float4 q;
+    float2 qp;
+};
+
+// The particle's feature row, from the plain density pass's records (its
+// (x, y, rho, rho_near), hit masks and stencil-row record, all in C order):
+// messages of the neighbours j with r/h < 1 (self excluded),
 // u = unit offset towards the neighbour, w = 1 - r/h,
 // dv = (v_j - v_i) dt / h with v = (x - x_prev) / dt:
 //   V1 = sum w u, V2 = sum w^2 u, M = sum w, T = sum w u u^T, D = sum w dv,
-// with the particle's rho, rho_near, neighbour count (r2 <= h2), its
-// scene's stiffness ratios a_k, a_n, a_s (k, k_near, k_spring over their
-// sum) and the three "own" terms of the relaxation formula
-// a_k (rho - rest) V1, a_n rho_near V2, a_s V1.  A particle with a
-// coincident neighbour (r2 <= 2e-12, where the reference nudges) or in an
-// overflowing bucket gets count 65535: it always takes the plain
-// relaxation.  Block 0 resets the step's fallback-list counter.
-// 40 registers: the occupancy this latency-bound gather gains is worth more
-// than the spills of its message sums (measured).
-__global__ void __maxnreg__(40)
-k_features(Ctx c, const float2 *__restrict__ pos, const float2 *__restrict__ prev,
-           const int *__restrict__ start, const unsigned *__restrict__ occ_in,
-           float4 *__restrict__ xr_out, ulonglong2 *__restrict__ mask01,
-           unsigned long long *__restrict__ mask2, int4 *__restrict__ rows_out,
-           __nv_bfloat16 *__restrict__ feat,
+//   R1 = sum w (rho_j - rest) u, R2 = sum w^2 rho_near_j u
+// (the neighbours' densities and near densities, as the relaxation's pair
+// term uses them, fluid.c:588-608), with the particle's rho, rho_near,
+// neighbour count (r2 <= h2), its scene's stiffness ratios a_k, a_n, a_s
+// (k, k_near, k_spring over their sum) and the "own" terms of the
+// relaxation formula a_k (rho - rest) V1, a_n rho_near V2, a_s V1.  A
+// particle with a coincident neighbour (r2 <= 2e-12, where the reference
+// nudges) or in an overflowing bucket gets count 65535: it always takes the
+// plain relaxation.  Block 0 resets the step's fallback-list counters.
+__global__ void __maxnreg__(48)
+k_messages(Ctx c, const float4 *__restrict__ xr, const ulonglong2 *__restrict__ mask01,
+           const unsigned long long *__restrict__ mask2, const int4 *__restrict__ rows,
+           const float2 *__restrict__ prev, const int *__restrict__ start,
+           const unsigned *__restrict__ occ_in, __nv_bfloat16 *__restrict__ feat,
            unsigned short *__restrict__ nbcount, unsigned *__restrict__ fb_count)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -96,139 +103,88 @@ k_features(Ctx c, const float2 *__restrict__ pos, const float2 *__restrict__ pre
         fb_count[1] = 0u;
     }
     if (i >= c.n) return;
+    // the particle's streams, requested together
+    const float4 me = xr[i];
+    const int4 rw = __ldg(rows + i);
+    const ulonglong2 m01 = __ldg(mask01 + i);
+    const unsigned long long m2 = __ldg(mask2 + i);
+    const float2 pp = prev[i];
     const Scene *S = c.scenes + scene_of(c, i);
-    const SG g = load_grid(S);
     const float hh = __ldg(&S->P.smoothing_radius);
     const float h2 = __fmul_rn(hh, hh);
     const float h_recip = __fdiv_rn(1.0f, hh);
     const float dt = __ldg(&S->P.time_step);
     const float inv_dt = 1.0f / dt;
     const float vscale = dt * h_recip;
+    const float rest = __ldg(&S->P.rest_density);
     const bool capped = *occ_in > (unsigned)c.max_bucket;
-    const float2 p = pos[i];
-    const float2 pp = prev[i];
+    const float2 p = make_float2(me.x, me.y);
     const float vix = (p.x - pp.x) * inv_dt, viy = (p.y - pp.y) * inv_dt;
     const float2 mp = make_float2(-p.x, -p.y);
-    const unsigned key = cell_key(p.x, p.y, g);
-    float2 ab = make_float2(0.0f, 0.0f);  // (rho, rho_near), as density_one's
-    unsigned long long m[3] = {0ull, 0ull, 0ull};
-    float2 V1 = make_float2(0.0f, 0.0f), V2 = V1, Tdiag = V1, Dsum = V1;
+    float2 V1 = make_float2(0.0f, 0.0f), V2 = V1, Tdiag = V1, Dsum = V1, R1 = V1, R2 = V1;
     float Ms = 0.0f, Txy = 0.0f;
     int count = 0;
-    bool degenerate = false;
-    int4 rec = make_int4(0, 0, 0, kRowsNone);  // as density_one's
-    if (searchable(key, i, start, g, capped, c.max_bucket)) {
-        rec.w = kRowsFull;
-        if (!capped) {
-            int ra[3], rl[3];
-            stencil_rows(key, start, g, ra, rl, c.n);
-            // one neighbour's terms (never the particle itself): density
-            // (add_density's rounding, so that the records equal the plain
-            // density pass's bit for bit), messages, counts
-            // qp: the neighbour's previous position
-            auto visit_p = [&](int j, const float2 &q, const float2 &qp) {
-                float2 e;  // q - p
-                const float r2 = dist2_packed(mp, q, e);
-                const float rinv = rsqrtf(r2);
-                const float ratio = __fmul_rn(__fsqrt_rn(r2), h_recip);
-                ++count;
-                degenerate |= r2 <= 2e-12f;
-                if (ratio < 1.0f) {
-                    const float omr = __fsub_rn(1.0f, ratio);
-                    const float omr2 = __fmul_rn(omr, omr);
-                    ab = __fadd2_rn(ab, make_float2(omr2, __fmul_rn(omr2, omr)));
-                    // message sums in packed FP32x2 arithmetic
-                    const float2 u = __fmul2_rn(e, make_float2(rinv, rinv));
-                    const float2 w2 = make_float2(omr, omr);
-                    const float2 wu = __fmul2_rn(w2, u);
-                    V1 = __fadd2_rn(V1, wu);
-                    V2 = __ffma2_rn(make_float2(omr2, omr2), u, V2);
-                    Ms += omr;
-                    Tdiag = __ffma2_rn(wu, u, Tdiag);
-                    Txy += wu.x * u.y;
-                    // sum w (x_j - x_prev_j); the velocities follow at the end
-                    Dsum = __ffma2_rn(w2, __fadd2_rn(q, make_float2(-qp.x, -qp.y)), Dsum);
-                }
-            };
-            auto visit = [&](int j, const float2 &q) { visit_p(j, q, __ldg(prev + j)); };
-            const int self = i - ra[1];  // the particle's own slot in row 1
-            if (rl[0] <= kMaskRow && rl[1] <= kMaskRow && rl[2] <= kMaskRow) {
-                rec = make_int4(ra[0], ra[1], ra[2], kRowsMasked);
-                // two phases, as the viscosity: the rows' hit masks from a
-                // cheap filter, then the heavy terms for the hits only, in
-                // the same (slot) order
-#pragma unroll
-                for (int r = 0; r < 3; ++r) {
-                    const float2 *row = pos + ra[r];
-                    const int len = rl[r];
-                    unsigned lo = 0u, hi = 0u;
-                    const int n0 = min(len, 32);
-                    for (int t = 0; t < n0; ++t) {
-                        float2 e;
-                        lo |= (unsigned)(dist2_packed(mp, __ldg(row + t), e) <= h2) << t;
-                    }
-                    for (int t = 32; t < len; ++t) {
-                        float2 e;
-                        hi |= (unsigned)(dist2_packed(mp, __ldg(row + t), e) <= h2) << (t - 32);
-                    }
-                    m[r] = ((unsigned long long)hi << 32) | lo;
-                }
-                m[1] &= ~(1ull << self);
-                // the walk loads each hit's position and previous position
-                // together, one hit ahead of its terms
-#pragma unroll
-                for (int r = 0; r < 3; ++r)
-                    walk_mask<float4>(
-                        m[r], ra[r], c.n,
-                        [&](int j) {
-                            const float2 q = __ldg(pos + j), qp = __ldg(prev + j);
-                            return make_float4(q.x, q.y, qp.x, qp.y);
-                        },
-                        [&](int j, const float4 &d) {
-                            visit_p(j, make_float2(d.x, d.y), make_float2(d.z, d.w));
-                        });
-            } else {
-                // a row longer than one mask (dense cells): one pass, the
-                // terms of each hit as the filter finds it, in slot order
-#pragma unroll
-                for (int r = 0; r < 3; ++r) {
-                    const float2 *row = pos + ra[r];
-                    unsigned long long mr = 0ull;
-                    for (int t = 0; t < rl[r]; ++t) {
-                        const float2 q = __ldg(row + t);
-                        float2 e;
-                        if (dist2_packed(mp, q, e) <= h2 && (r != 1 || t != self)) {
-                            if (t < kMaskRow) mr |= 1ull << t;
-                            visit(ra[r] + t, q);
-                        }
-                    }
-                    m[r] = mr;
-                }
-            }
-        } else {
-            degenerate = true;
-            for_each_candidate(key, start, g, true, c.max_bucket, c.n, [&](int j) {
-                if (j == i) return;
-                const float2 q = __ldg(pos + j);
-                const float r2 = dist2(p.x - q.x, p.y - q.y);
-                if (r2 > h2) return;
-                add_density(ab, r2, h_recip);
-            });
+    bool degenerate = capped;
+    // one neighbour (r2 <= h2 known, never the particle itself)
+    auto visit = [&](int, const NbRec &d) {
+        float2 e;  // q - p
+        const float r2 = dist2_packed(mp, make_float2(d.q.x, d.q.y), e);
+        const float rinv = rsqrtf(r2);
+        const float ratio = r2 * rinv * h_recip;
+        ++count;
+        degenerate |= r2 <= 2e-12f;
+        if (ratio < 1.0f) {
+            const float omr = 1.0f - ratio;
+            const float omr2 = omr * omr;
+            // message sums in packed FP32x2 arithmetic
+            const float2 u = __fmul2_rn(e, make_float2(rinv, rinv));
+            const float2 w2 = make_float2(omr, omr);
+            const float2 wu = __fmul2_rn(w2, u);
+            V1 = __fadd2_rn(V1, wu);
+            V2 = __ffma2_rn(make_float2(omr2, omr2), u, V2);
+            Ms += omr;
+            Tdiag = __ffma2_rn(wu, u, Tdiag);
+            Txy += wu.x * u.y;
+            const float pr = d.q.z - rest, prn = omr2 * d.q.w;
+            R1 = __ffma2_rn(make_float2(pr, pr), wu, R1);
+            R2 = __ffma2_rn(make_float2(prn, prn), u, R2);
+            // sum w (x_j - x_prev_j); the velocities follow at the end
+            Dsum = __ffma2_rn(w2, __fadd2_rn(make_float2(d.q.x, d.q.y),
+                                             make_float2(-d.qp.x, -d.qp.y)), Dsum);
         }
+    };
+    auto load = [&](int j) {
+        NbRec d;
+        d.q = __ldg(xr + j);
+        d.qp = __ldg(prev + j);
+        return d;
+    };
+    if (!capped && rw.w == kRowsMasked) {
+        const int ra[3] = {rw.x, rw.y, rw.z};
+        const unsigned long long mm[3] = {m01.x, m01.y, m2};
+#pragma unroll
+        for (int r = 0; r < 3; ++r) walk_mask<NbRec>(mm[r], ra[r], c.n, load, visit);
+    } else if (!capped && rw.w == kRowsFull) {
+        // a stencil row longer than a hit mask: the whole stencil, in slot
+        // order
+        const SG g = load_grid(S);
+        const unsigned key = cell_key(p.x, p.y, g);
+        for_each_candidate(key, start, g, false, c.max_bucket, c.n, [&](int j) {
+            if (j == i) return;
+            const NbRec d = load(j);
+            float2 e;
+            if (dist2_packed(mp, make_float2(d.q.x, d.q.y), e) > h2) return;
+            visit(j, d);
+        });
     }
-    const float a = ab.x, b = ab.y;
-    xr_out[i] = make_float4(p.x, p.y, a, b);
-    mask01[i] = make_ulonglong2(m[0], m[1]);
-    mask2[i] = m[2];
-    rows_out[i] = rec;
     nbcount[i] = degenerate ? (unsigned short)65535 : (unsigned short)(count < 65534 ? count : 65534);
+    const float a = me.z, b = me.w;
     const float V1x = V1.x, V1y = V1.y, V2x = V2.x, V2y = V2.y;
     const float Txx = Tdiag.x, Tyy = Tdiag.y;
     // sum w (v_j - v_i) = (sum w (x_j - x_prev_j)) / dt - v_i sum w
     const float Dx = Dsum.x * inv_dt - vix * Ms, Dy = Dsum.y * inv_dt - viy * Ms;
 
     const float k = __ldg(&S->P.k), kn = __ldg(&S->P.k_near), ks = __ldg(&S->P.k_spring);
-    const float rest = __ldg(&S->P.rest_density);
     const float ksum = k + kn + ks;
     const float ak = k / ksum, an = kn / ksum, as = ks / ksum;
     const float ds = vscale * 2.5f;
@@ -256,8 +212,12 @@ k_features(Ctx c, const float2 *__restrict__ pos, const float2 *__restrict__ pre
     f[20] = an * b * V2y * 0.5f;
     f[21] = as * V1x * 0.5f;
     f[22] = as * V1y * 0.5f;
+    f[23] = ak * R1.x * 0.25f;
+    f[24] = ak * R1.y * 0.25f;
+    f[25] = an * R2.x * 0.5f;
+    f[26] = an * R2.y * 0.5f;
 #pragma unroll
-    for (int e = 23; e < IN - 1; ++e) f[e] = 0.0f;
+    for (int e = 27; e < IN - 1; ++e) f[e] = 0.0f;
     f[IN - 1] = 1.0f;  // constant input: the first layer's bias
     uint4 *row = reinterpret_cast<uint4 *>(feat + (size_t)i * IN);
 #pragma unroll
@@ -1022,16 +982,16 @@ int train_loop(LearnedModel *l, int first, int nsamples, int epochs, int batch, 
     return SPH_OK;
 }
 
-// Feature pass on the handle's C order into (feat, nbc); density records and
-// hit masks into the handle's own C-order arrays (the values the plain
-// density pass writes there).
-int launch_features(sph_cuda *h, __nv_bfloat16 *feat, unsigned short *nbc)
+// Message pass on the handle's C order into (feat, nbc), from the density
+// records and hit masks the density pass has just left in the handle's
+// C-order arrays.
+int launch_messages(sph_cuda *h, __nv_bfloat16 *feat, unsigned short *nbc)
 {
     if (h->n == 0) return SPH_OK;
-    ml::k_features<<<nblk(h->n), kBlock, 0, h->stream>>>(
-        make_ctx(h), h->pos_c, h->prev_c, h->start_c, &h->d_state->build_max_occ[SLOT_PREDICTED],
-        h->xr_c, h->mask01_c, h->mask2_c, h->rows_c, feat, nbc, &h->d_state->fb_count);
-    return cuda_fail(cudaGetLastError(), "features");
+    ml::k_messages<<<nblk(h->n), kBlock, 0, h->stream>>>(
+        make_ctx(h), h->xr_c, h->mask01_c, h->mask2_c, h->rows_c, h->prev_c, h->start_c,
+        &h->d_state->build_max_occ[SLOT_PREDICTED], feat, nbc, &h->d_state->fb_count);
+    return cuda_fail(cudaGetLastError(), "messages");
 }
 
 int run_mlp(cudaStream_t st, LearnedModel *l, int n, const __nv_bfloat16 *feat, float4 *out,
@@ -1062,8 +1022,8 @@ int ensure_learned_buffers(sph_cuda *h)
 int predicted_features(sph_cuda *h, LearnedModel *l)
 {
     LTRY(ensure_learned_buffers(h));
-    LTRY(enqueue_predicted_state(h));
-    LTRY(launch_features(h, (__nv_bfloat16 *)h->feat_c, h->nbc_c));
+    LTRY(enqueue_predicted_state(h));  // ends with the density pass
+    LTRY(launch_messages(h, (__nv_bfloat16 *)h->feat_c, h->nbc_c));
     if (l) {
         LCUDA(cudaStreamSynchronize(l->stream));  // weights written on the model's stream
         LTRY(run_mlp(h->stream, l, h->n, (const __nv_bfloat16 *)h->feat_c, h->net_c, h->num_sms));
@@ -1074,13 +1034,14 @@ int predicted_features(sph_cuda *h, LearnedModel *l)
 }  // namespace
 
 // Learned passes of a step (called by enqueue_step when a model is
-// attached): features (density + messages) on the C order, then the
-// network.  With `events`, events[0] is recorded after the features and
-// events[1] after the network.
+// attached): the features (the plain density pass, then the message pass)
+// on the C order, then the network.  With `events`, events[0] is recorded
+// after the features and events[1] after the network.
 int launch_learned_passes(sph_cuda *h, cudaEvent_t *events)
 {
     LearnedModel *l = h->learned;
-    LTRY(launch_features(h, (__nv_bfloat16 *)h->feat_c, h->nbc_c));
+    LTRY(launch_density_pass(h));
+    LTRY(launch_messages(h, (__nv_bfloat16 *)h->feat_c, h->nbc_c));
     if (events) cudaEventRecord(events[0], h->stream);
     LTRY(run_mlp(h->stream, l, h->n, (const __nv_bfloat16 *)h->feat_c, h->net_c, h->num_sms));
     if (events) cudaEventRecord(events[1], h->stream);

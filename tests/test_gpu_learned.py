@@ -106,30 +106,42 @@ def numpy_features(sc):
     cnt = np.zeros(n, np.int64)
     k, kn, ks, rest = P.k, P.k_near, P.k_spring, P.rest_density
     ak, an, as_ = k / (k + kn + ks), kn / (k + kn + ks), ks / (k + kn + ks)
+    # every particle's neighbours and densities first: the messages carry
+    # the neighbours' densities and near densities
+    nbs, ws, us = [], [], []
+    rho, rhon = np.zeros(n), np.zeros(n)
     for i in range(n):
         dx = (px - px[i]).astype(np.float32)
         dy = (py - py[i]).astype(np.float32)
         r2 = (dx * dx + dy * dy).astype(np.float32)
         nb = np.nonzero(r2 <= np.float32(h * h))[0]
         nb = nb[nb != i]
-        cnt[i] = len(nb)
         r = np.sqrt(r2[nb].astype(np.float64))
         q = r / h
-        inside = q < 1
-        w = np.where(inside, 1.0 - q, 0.0)
-        ux, uy = dx[nb] / r, dy[nb] / r
-        a = np.sum(w * w)
-        b = np.sum(w ** 3)
+        w = np.where(q < 1, 1.0 - q, 0.0)
+        nbs.append(nb)
+        ws.append(w)
+        us.append((dx[nb] / r, dy[nb] / r))
+        rho[i], rhon[i] = np.sum(w * w), np.sum(w ** 3)
+    for i in range(n):
+        nb, w, (ux, uy) = nbs[i], ws[i], us[i]
+        cnt[i] = len(nb)
+        a, b = rho[i], rhon[i]
         dvx = (vx[nb] - vx[i]) * dt / h
         dvy = (vy[nb] - vy[i]) * dt / h
         V1 = (np.sum(w * ux), np.sum(w * uy))
         V2 = (np.sum(w * w * ux), np.sum(w * w * uy))
+        pr = w * (rho[nb] - rest)
+        prn = w * w * rhon[nb]
+        R1 = (np.sum(pr * ux), np.sum(pr * uy))
+        R2 = (np.sum(prn * ux), np.sum(prn * uy))
         f = [a / 4, b / 2, V1[0] / 4, V1[1] / 4, V2[0] / 2, V2[1] / 2, np.sum(w) / 8,
              min(len(nb), 48) / 48, np.sum(w * dvx) * 2.5, np.sum(w * dvy) * 2.5,
              np.sum(w * ux * ux) / 4, np.sum(w * ux * uy) / 4, np.sum(w * uy * uy) / 4,
              ak, an, as_, rest / 4,
              ak * (a - rest) * V1[0] / 4, ak * (a - rest) * V1[1] / 4,
-             an * b * V2[0] / 2, an * b * V2[1] / 2, as_ * V1[0] / 2, as_ * V1[1] / 2]
+             an * b * V2[0] / 2, an * b * V2[1] / 2, as_ * V1[0] / 2, as_ * V1[1] / 2,
+             ak * R1[0] / 4, ak * R1[1] / 4, an * R2[0] / 2, an * R2[1] / 2]
         f += [0.0] * (31 - len(f)) + [1.0]
         out[i] = f
     return out, cnt
