@@ -443,7 +443,7 @@ def train_learned(args):
     return m, info
 
 
-def run_learned(args, work, plain_ms, shapes):
+def run_learned(args, work, plain_ms, shapes, long_masks=False):
     """The learned step on the dam break: throughput (CUDA events around
     graph-launched steps), one-step RMS density error against the plain step
     from the same state, the fallback share, and a 1,000-step trajectory's
@@ -454,6 +454,7 @@ def run_learned(args, work, plain_ms, shapes):
     K, W = args.steps, args.warmup
     sim = work.fresh()
     sim.set_launch_shapes(shapes)
+    sim.set_long_row_masks(long_masks)
     work.advance(sim, 0, W)
     sim.set_learned(model, thr)
     work.advance(sim, W, 5)
@@ -540,9 +541,11 @@ def run_skewed(args, world, rank):
         tuner = fresh(label == "learned")
         tuner.step(None, W + K // 2)
         shapes = tuner.autotune(3)
+        long_masks = tuner.long_row_masks()
         tuner.close()
         e = fresh(label == "learned")
         e.set_launch_shapes(shapes)
+        e.set_long_row_masks(long_masks)
         e.step(None, W)
         e.synchronize()
         barrier(world)
@@ -552,7 +555,7 @@ def run_skewed(args, world, rank):
             ms = e.timer_stop()
         ms = max_over_ranks(world, ms)
         kt = [e.kernel_times(None) for _ in range(3)]
-        res[label] = {"ms": ms, "clocks": clk.summary(), "shapes": shapes,
+        res[label] = {"ms": ms, "clocks": clk.summary(), "shapes": shapes, "long_masks": long_masks,
                       "launches": e.launches_per_step() * K,
                       "kernel_ms": {k: round(statistics.median(r[k] for r in kt), 5) for k in kt[0]},
                       "counts": e.learned_counts() if label == "learned" else None}
@@ -593,7 +596,8 @@ def run_skewed(args, world, rank):
                                        f"learned relaxation",
                            "particles": n, "cells": cells, "settle_s": t_settle,
                            "max_cell_occupancy_first_256": max(occ),
-                           "parallelism": f"replicas x{world}", "launch_shapes": L["shapes"]},
+                           "parallelism": f"replicas x{world}", "launch_shapes": L["shapes"],
+                           "long_row_masks": L["long_masks"]},
                 "plain": {"value": world * n * K / (P["ms"] / 1e3), "ms_per_step": P["ms"] / K,
                           "kernel_ms": P["kernel_ms"], "clocks": P["clocks"]},
                 "learned_vs_plain": P["ms"] / L["ms"],
@@ -697,16 +701,19 @@ def run_gpu(args, world, rank):
     # the middle of the timed window (the gathers' costs drift as a scene
     # compresses), so that the timed steps are steps W .. W+K-1 of the run ----
     if args.shapes:
-        shapes = [int(v) for v in args.shapes.split(",")]
+        given = [int(v) for v in args.shapes.split(",")]
+        shapes, long_masks = given[:6], bool(given[6]) if len(given) > 6 else False
     else:
         tuner = work.fresh()
         work.advance(tuner, 0, W + K // 2)
         shapes = work.tune(tuner)
+        long_masks = tuner.long_row_masks()
         tuner.close()
 
     # ---- device-resident throughput ----
     sim = work.fresh()
     sim.set_launch_shapes(shapes)
+    sim.set_long_row_masks(long_masks)
     work.advance(sim, 0, W)
     t0 = W
     sim.synchronize()
@@ -781,6 +788,7 @@ def run_gpu(args, world, rank):
             staged.append(pa)
         sim2 = work.blank()
         sim2.set_launch_shapes(shapes)
+        sim2.set_long_row_masks(long_masks)
         sim2.synchronize()
         tw = time.perf_counter()
         sim2.upload(*[pa.array for pa in staged])
@@ -812,7 +820,7 @@ def run_gpu(args, world, rank):
     learned = None
     if args.workload == "dam_break" and not args.no_learned:
         try:
-            learned = run_learned(args, work, ms / K, shapes)
+            learned = run_learned(args, work, ms / K, shapes, long_masks)
         except Exception as exc:  # reported, never hidden
             learned = {"error": f"{type(exc).__name__}: {exc}"}
 
@@ -824,7 +832,8 @@ def run_gpu(args, world, rank):
                 "config": {"workload": work.name,
                            "particles": n, "cells": cells, "parallelism": f"replicas x{world}",
                            "l2": "no flush: per-step working set ~0.5 GB > 129 MB L2",
-                           "steps_timed": f"{t0}..{t0 + K - 1}", "launch_shapes": shapes},
+                           "steps_timed": f"{t0}..{t0 + K - 1}", "launch_shapes": shapes,
+                           "long_row_masks": long_masks},
                 "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
                 "parity": parity, "late_window": late,
                 "clocks": clocks, "gpu_launches": launches, "learned": learned,
@@ -848,8 +857,9 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=12)
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--shapes", default="",
-                    help="six ints: the gathers' launch shapes, instead of autotuning "
-                         "(profiling runs: under a profiler the tuner's timings are not real)")
+                    help="six ints: the gathers' launch shapes, and optionally a seventh, 1 for "
+                         "long-row hit masks, instead of autotuning (profiling runs: under a "
+                         "profiler the tuner's timings are not real)")
     ap.add_argument("--no-trajectory", action="store_true")
     ap.add_argument("--no-parity", action="store_true")
     ap.add_argument("--late-start", type=int, default=480,

@@ -143,12 +143,24 @@ int sph_cuda_scene_diagnostics(sph_cuda_t *h, double *out);
 int sph_cuda_set_launch_shapes(sph_cuda_t *h, const int *shapes);
 int sph_cuda_get_launch_shapes(sph_cuda_t *h, int *shapes);
 
+/* Long-row hit masks (off after create): the density pass also records the
+ * neighbours among candidates 65..128 of a stencil row, so that the
+ * relaxation (and the learned step's message walk) walks hit masks instead
+ * of the whole stencil for particles in cells dense enough for such rows.
+ * Results are bit for bit the same either way (the same pairs, in the same
+ * order); the masks take 24 bytes per particle of device memory, allocated
+ * on the first switch on.  They pay in dense scenes and cost a little where
+ * long rows are rare; sph_cuda_autotune chooses. */
+int sph_cuda_set_long_row_masks(sph_cuda_t *h, int on);
+int sph_cuda_get_long_row_masks(sph_cuda_t *h);
+
 /* Autotuner: for each gather in turn (the others at their best so far),
  * times one graph-launched step per candidate shape over trial_steps
  * interleaved rounds and keeps the candidate with the lowest median step
- * time.  It advances the simulation by 48 x trial_steps steps (each
- * measurement re-captures the step graph with one untimed step first); the
- * chosen shapes go to shapes_out (6 ints) if given. */
+ * time; then chooses long-row masks on or off the same way.  It advances
+ * the simulation by 50 x trial_steps steps (each measurement re-captures
+ * the step graph with one untimed step first); the chosen shapes go to
+ * shapes_out (6 ints) if given. */
 int sph_cuda_autotune(sph_cuda_t *h, int trial_steps, int *shapes_out);
 
 /* Frees all device and host resources of the handle. */

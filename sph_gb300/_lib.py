@@ -128,6 +128,8 @@ _SIGS = {
     "sph_cuda_set_launch_shapes": (ctypes.c_int, [_P, c_int_p]),
     "sph_cuda_get_launch_shapes": (ctypes.c_int, [_P, c_int_p]),
     "sph_cuda_autotune": (ctypes.c_int, [_P, ctypes.c_int, c_int_p]),
+    "sph_cuda_set_long_row_masks": (ctypes.c_int, [_P, ctypes.c_int]),
+    "sph_cuda_get_long_row_masks": (ctypes.c_int, [_P]),
     "sph_cuda_set_stream": (ctypes.c_int, [_P, _P]),
     "sph_cuda_upload": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.POINTER(FluidParticle)), ctypes.c_int]),
     "sph_cuda_upload_particles": (ctypes.c_int, [_P, _P, ctypes.c_int]),

@@ -228,7 +228,7 @@ static void free_all(sph_cuda *h)
     }
     if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
     void *ptrs[] = {h->pos_a, h->vel_a, h->id_a, h->pos_b, h->prev_b, h->vel_b, h->kr_b,
-                    h->pos_c, h->prev_c, h->xr_c, h->mask01_c, h->mask2_c, h->rows_c, h->id_c,
+                    h->pos_c, h->prev_c, h->xr_c, h->mask01_c, h->mask2_c, h->maskx_c, h->rows_c, h->id_c,
                     h->tmp_id, h->cnt, h->start_a, h->start_c, h->tile_sums, h->build_tiles, h->d_scenes,
                     h->d_p_off, h->d_nocell, h->d_state, h->d_partials, h->d_scratch};
     for (void *p : ptrs)
@@ -1140,6 +1140,24 @@ int sph_cuda_set_launch_shapes(sph_cuda_t *h, const int *shapes)
     return SPH_OK;
 }
 
+int sph_cuda_set_long_row_masks(sph_cuda_t *h, int on)
+{
+    SPH_TRY(check_handle(h));
+    if (on && !long_masks_supported()) {
+        set_error("long-row masks are not built with the shared-memory staged gathers");
+        return SPH_ERR_UNSUPPORTED;
+    }
+    if (on && !h->maskx_c) SPH_TRY(dalloc(&h->maskx_c, 3 * (size_t)h->capacity + 3));
+    if ((on != 0) != h->long_masks) {
+        SPH_CUDA(cudaStreamSynchronize(h->stream));
+        h->long_masks = on != 0;
+        destroy_graph(h);
+    }
+    return SPH_OK;
+}
+
+int sph_cuda_get_long_row_masks(sph_cuda_t *h) { return h && h->long_masks ? 1 : 0; }
+
 int sph_cuda_get_launch_shapes(sph_cuda_t *h, int *shapes)
 {
     SPH_TRY(check_handle(h));
@@ -1207,6 +1225,32 @@ int sph_cuda_autotune(sph_cuda_t *h, int trial_steps, int *shapes_out)
         }
     }
     for (int k = 0; k < kGathers; ++k) h->shape[k] = pick[k];
+    // then the long-row hit masks, on or off, the same way (they pay where
+    // stencil rows of more than 64 candidates are common, and cost a little
+    // where they are not)
+    if (long_masks_supported()) {
+        const bool was = h->long_masks;
+        if (sph_cuda_set_long_row_masks(h, 1) == SPH_OK) {
+            std::vector<float> t[2];
+            for (int r = 0; r < trial_steps; ++r)
+                for (int v = 0; v < 2; ++v) {
+                    h->long_masks = v != 0;
+                    destroy_graph(h);
+                    SPH_TRY(run_steps(h, 1));
+                    SPH_CUDA(cudaEventRecord(h->timer[0], h->stream));
+                    SPH_TRY(run_steps(h, 1));
+                    SPH_CUDA(cudaEventRecord(h->timer[1], h->stream));
+                    SPH_CUDA(cudaEventSynchronize(h->timer[1]));
+                    float ms = 0.0f;
+                    SPH_CUDA(cudaEventElapsedTime(&ms, h->timer[0], h->timer[1]));
+                    t[v].push_back(ms);
+                }
+            for (auto &v : t) std::sort(v.begin(), v.end());
+            h->long_masks = t[1][t[1].size() / 2] < t[0][t[0].size() / 2];
+        } else {
+            h->long_masks = was;
+        }
+    }
     destroy_graph(h);
     if (shapes_out) SPH_TRY(sph_cuda_get_launch_shapes(h, shapes_out));
     return SPH_OK;

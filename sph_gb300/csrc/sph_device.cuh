@@ -383,7 +383,9 @@ constexpr int kMaskRow = 64;  // candidates per stencil row recorded in a hit ma
 // (w): kRowsNone, no neighbours (out of the grid or beyond the bucket cap);
 // kRowsMasked, walk the hit masks from those slots; kRowsFull, search the
 // whole stencil again (a row longer than kMaskRow, or an overflowing bucket).
-constexpr int kRowsNone = 0, kRowsMasked = 1, kRowsFull = 2;
+// kRowsMasked2: as kRowsMasked for rows of up to 2 kMaskRow candidates, the
+// bits of candidates kMaskRow.. in Ctx::maskx (long-row masks).
+constexpr int kRowsNone = 0, kRowsMasked = 1, kRowsFull = 2, kRowsMasked2 = 3;
 
 // Visits the set bits of a 64-bit row mask in increasing order with one
 // neighbour's data in flight: load(j) for slot base + t of the next bit is

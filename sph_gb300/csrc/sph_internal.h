@@ -44,6 +44,10 @@ struct Ctx {
     // particles per scan tile of the build that the kernel's cell keys feed,
     // counted by the step's key producers (null: not counted)
     unsigned *tile_cnt = nullptr;
+    // long-row hit masks (kernels built for them only): per particle, 3
+    // words holding the hit bits of candidates kMaskRow..2 kMaskRow - 1 of
+    // each stencil row (null: rows longer than kMaskRow are not masked)
+    unsigned long long *maskx = nullptr;
 };
 
 // Device-resident counters and flags of one handle.
@@ -118,6 +122,9 @@ struct sph_cuda {
     float4 *xr_c = nullptr;               // (x, y, rho, rho_near) of the density pass
     ulonglong2 *mask01_c = nullptr;       // neighbour hit masks of stencil rows 0, 1
     unsigned long long *mask2_c = nullptr;  // ... and row 2
+    // long-row hit masks (sph_cuda_set_long_row_masks): 3 words per particle
+    bool long_masks = false;
+    unsigned long long *maskx_c = nullptr;
     int4 *rows_c = nullptr;               // the stencil rows' first slots and walk mode
     int *id_c = nullptr;
     int *tmp_id = nullptr;
@@ -188,6 +195,7 @@ inline Ctx make_ctx(const sph_cuda *h)
     c.max_bucket = h->max_bucket;
     c.M = h->M;
     c.tile_cnt = h->build_tiles;
+    c.maskx = h->long_masks ? h->maskx_c : nullptr;
     return c;
 }
 
@@ -205,6 +213,7 @@ unsigned bounds_flags_kernels();  // checked builds (SPH_BOUNDS_CHECK): recorded
 unsigned bounds_flags_learned();
 int enqueue_predicted_state(sph_cuda *h);       // first half of a step: C order + density
 int launch_density_pass(sph_cuda *h);            // the density pass on the C order
+bool long_masks_supported();
 int launch_learned_passes(sph_cuda *h, cudaEvent_t *events);  // features + network (C order)
 int launch_learned_relax(sph_cuda *h, float2 *probe_out, cudaEvent_t *events = nullptr);
 void free_learned_buffers(sph_cuda *h);

@@ -841,11 +841,14 @@ k_viscosity_predict(Ctx c, const DevState *__restrict__ st, const float2 *__rest
 // The candidate filter of one particle over its three stencil rows (slots
 // [ra[r], ra[r] + rl[r])), reading the rows from global memory or, SM, from
 // the CTA's shared-memory copy (slot j of row r at base[j + d[r]]).
+// mx (long-row masks): where the hit bits of candidates kMaskRow..
+// 2 kMaskRow - 1 of each row go (3 words; null: nowhere).
 template <bool SM>
 __device__ __forceinline__ void density_filter(int i, float2 mp, float h2, float h_recip,
                                                const int (&ra)[3], const int (&rl)[3],
                                                const float2 *base, const int (&d)[3],
-                                               float2 &ab, unsigned long long (&m)[3])
+                                               float2 &ab, unsigned long long (&m)[3],
+                                               unsigned long long *mx = nullptr)
 {
     // the particle's own slot in its row (row 1): never a neighbour of
     // itself (hash.c pairs distinct particles only)
@@ -869,9 +872,24 @@ __device__ __forceinline__ void density_filter(int i, float2 mp, float h2, float
                 }
             }
         }
-        // rows longer than the mask (the relaxation then walks the whole
-        // stencil): the remaining candidates, no mask bits
-        for (int t = kMaskRow; t < len; ++t) {
+        // rows longer than the mask: with long-row masks the next kMaskRow
+        // candidates' bits go to mx; the rest have no mask bits (the
+        // relaxation then walks the whole stencil)
+        int t2 = kMaskRow;
+        if (mx != nullptr && len > kMaskRow) {
+            unsigned long long hx = 0ull;
+            t2 = min(len, 2 * kMaskRow);
+            for (int t = kMaskRow; t < t2; ++t) {
+                float2 e;
+                const float r2 = dist2_packed(mp, at(t), e);
+                if (r2 <= h2 && (r != 1 || t != self)) {
+                    hx |= 1ull << (t - kMaskRow);
+                    add_density(ab, r2, h_recip);
+                }
+            }
+            mx[r] = hx;
+        }
+        for (int t = t2; t < len; ++t) {
             float2 e;
             const float r2 = dist2_packed(mp, at(t), e);
             if (r2 <= h2 && (r != 1 || t != self)) add_density(ab, r2, h_recip);
@@ -883,7 +901,9 @@ __device__ __forceinline__ void density_filter(int i, float2 mp, float h2, float
 // STAGED: every thread of the CTA calls this (also those with no particle,
 // valid = false), and the CTA first copies the union of its stencil rows to
 // shared memory `sm` (cap elements; stage_rows).
-template <bool STAGED = false>
+// LM: long-row masks (rows of up to 2 kMaskRow candidates recorded as
+// kRowsMasked2, their second masks in c.maskx).
+template <bool STAGED = false, bool LM = false>
 __device__ __forceinline__ void density_one(int i, const Ctx &c, const float2 *__restrict__ pos,
                                             const int *__restrict__ start, bool capped,
                                             float4 *__restrict__ xr_out,
@@ -922,12 +942,19 @@ __device__ __forceinline__ void density_one(int i, const Ctx &c, const float2 *_
     if (search) {
         rec.w = kRowsFull;
         if (!capped) {
-            if (rl[0] <= kMaskRow && rl[1] <= kMaskRow && rl[2] <= kMaskRow)
+            unsigned long long *mx = nullptr;
+            if (rl[0] <= kMaskRow && rl[1] <= kMaskRow && rl[2] <= kMaskRow) {
                 rec = make_int4(ra[0], ra[1], ra[2], kRowsMasked);
+            } else if (LM && !STAGED && c.maskx && rl[0] <= 2 * kMaskRow &&
+                       rl[1] <= 2 * kMaskRow && rl[2] <= 2 * kMaskRow) {
+                rec = make_int4(ra[0], ra[1], ra[2], kRowsMasked2);
+                mx = c.maskx + 3 * (size_t)i;
+                mx[0] = mx[1] = mx[2] = 0ull;  // rows of kMaskRow or fewer leave theirs
+            }
             if (STAGED && staged)
                 density_filter<true>(i, mp, h2, h_recip, ra, rl, sm, d, ab, m);
             else
-                density_filter<false>(i, mp, h2, h_recip, ra, rl, pos, d, ab, m);
+                density_filter<false>(i, mp, h2, h_recip, ra, rl, pos, d, ab, m, LM ? mx : nullptr);
         } else {
             for_each_candidate(key, start, g, true, c.max_bucket, c.n, [&](int j) {
                 if (j == i) return;
@@ -969,7 +996,7 @@ k_density_sm(Ctx c, const float2 *__restrict__ pos, const int *__restrict__ star
 #ifndef SPH_DENS_MIN_BLOCKS
 #define SPH_DENS_MIN_BLOCKS 4  // resident 512-thread CTAs per SM the density pass is built for
 #endif
-template <bool PERSIST>
+template <bool PERSIST, bool LM = false>
 __global__ void __launch_bounds__(kMaxBlock, SPH_DENS_MIN_BLOCKS)
 k_density_t(Ctx c, const float2 *__restrict__ pos, const int *__restrict__ start,
             const unsigned *__restrict__ occ_in, float4 *__restrict__ xr_out,
@@ -980,11 +1007,12 @@ k_density_t(Ctx c, const float2 *__restrict__ pos, const int *__restrict__ start
     const bool capped = *occ_in > (unsigned)c.max_bucket;
     const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
     if (!PERSIST) {
-        if (i0 < c.n) density_one(i0, c, pos, start, capped, xr_out, mask01, mask2, rows_out);
+        if (i0 < c.n)
+            density_one<false, LM>(i0, c, pos, start, capped, xr_out, mask01, mask2, rows_out);
         return;
     }
     for (int i = i0; i < c.n; i += gridDim.x * blockDim.x)
-        density_one(i, c, pos, start, capped, xr_out, mask01, mask2, rows_out);
+        density_one<false, LM>(i, c, pos, start, capped, xr_out, mask01, mask2, rows_out);
 }
 
 // One density launch per block (the form other translation units call).
@@ -1175,7 +1203,7 @@ __device__ __forceinline__ void relax_finish(int i, const Ctx &cx, const Scene *
     kr_out[i] = make_uint2(k2, rank);
 }
 
-template <bool PROBE, bool LEARNED = false, bool LONG_ROWS = false>
+template <bool PROBE, bool LEARNED = false, bool LONG_ROWS = false, bool LM = false>
 __device__ __forceinline__ void relax_update_one(
     int i, const Ctx &cx, const float4 *__restrict__ xr, const ulonglong2 *__restrict__ mask01,
     const unsigned long long *__restrict__ mask2, const int4 *__restrict__ rows,
@@ -1263,7 +1291,25 @@ __device__ __forceinline__ void relax_update_one(
             }
         }
     }
-    if (mode == kRowsMasked) {
+    if (LM && mode == kRowsMasked2) {
+        // rows of up to 2 kMaskRow candidates: each row's two masks in slot
+        // order (the visiting order of the whole-stencil walk)
+        const ulonglong2 m01 = kHoist ? m01h : mask01[i];
+        const unsigned long long mm[3] = {m01.x, m01.y, kHoist ? m2h : mask2[i]};
+        const unsigned long long *mx = cx.maskx + 3 * (size_t)i;
+        const unsigned long long mh[3] = {__ldg(mx), __ldg(mx + 1), __ldg(mx + 2)};
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+#pragma unroll
+            for (int q = 0; q < 2; ++q)
+                walk_mask<float4>(
+                    q ? mh[r] : mm[r], ra[r] + q * kMaskRow, cx.n,
+                    [&](int j) { return __ldg(xr + j); },
+                    [&](int j, const float4 &qv) {
+                        relax_pair_walk(wc, p, qv, i, j, S, ids, acc, nudges);
+                    });
+        }
+    } else if (mode == kRowsMasked) {
         const ulonglong2 m01 = kHoist ? m01h : mask01[i];
         const unsigned long long mm[3] = {m01.x, m01.y, kHoist ? m2h : mask2[i]};
         if (R.sm) {
@@ -1351,7 +1397,7 @@ k_relax_update_sm(Ctx c, const float4 *__restrict__ xr, const ulonglong2 *__rest
     }
 }
 
-template <bool PROBE, bool PERSIST = false>
+template <bool PROBE, bool PERSIST = false, bool LM = false>
 __global__ void __launch_bounds__(kBlock, SPH_RELAX_MIN_BLOCKS)
 k_relax_update(Ctx c, const float4 *__restrict__ xr, const ulonglong2 *__restrict__ mask01,
                const unsigned long long *__restrict__ mask2, const int4 *__restrict__ rows,
@@ -1368,13 +1414,15 @@ k_relax_update(Ctx c, const float4 *__restrict__ xr, const ulonglong2 *__restric
     const bool capped = *occ_in > (unsigned)c.max_bucket;
     if (!PERSIST) {
         if (i0 < c.n)
-            relax_update_one<PROBE>(i0, c, xr, mask01, mask2, rows, prev, ids, start, capped, pos_out,
-                                    vel_out, kr_out, cnt, probe_out);
+            relax_update_one<PROBE, false, false, LM>(i0, c, xr, mask01, mask2, rows, prev, ids,
+                                                      start, capped, pos_out, vel_out, kr_out,
+                                                      cnt, probe_out);
         return;
     }
     for (int i = i0; i < c.n; i += gridDim.x * blockDim.x)
-        relax_update_one<PROBE>(i, c, xr, mask01, mask2, rows, prev, ids, start, capped, pos_out,
-                                vel_out, kr_out, cnt, probe_out);
+        relax_update_one<PROBE, false, false, LM>(i, c, xr, mask01, mask2, rows, prev, ids, start,
+                                                  capped, pos_out, vel_out, kr_out, cnt,
+                                                  probe_out);
 }
 
 // The relaxation pass of a learned step (one particle per thread).  PROBE:
@@ -1382,7 +1430,7 @@ k_relax_update(Ctx c, const float4 *__restrict__ xr, const ulonglong2 *__restric
 // that take the network are advanced here and the others are appended to
 // fb_list (one atomic per warp that has any) for k_relax_fallback, so that
 // the rare plain gathers do not hold up whole warps.  Block 0 counts the step.
-template <bool PROBE>
+template <bool PROBE, bool LM = false>
 __global__ void __launch_bounds__(kBlock, 4)
 k_relax_learned(Ctx c, const float4 *__restrict__ xr, const ulonglong2 *__restrict__ mask01,
                 const unsigned long long *__restrict__ mask2, const int4 *__restrict__ rows,
@@ -1403,7 +1451,7 @@ k_relax_learned(Ctx c, const float4 *__restrict__ xr, const ulonglong2 *__restri
     L.defer = !PROBE;
     int t = -1;
     if (i < c.n)
-        relax_update_one<PROBE, true>(i, c, xr, mask01, mask2, rows, prev, ids, start, capped, pos_out,
+        relax_update_one<PROBE, true, false, LM>(i, c, xr, mask01, mask2, rows, prev, ids, start, capped, pos_out,
                                       vel_out, kr_out, cnt, probe_out, L, &used, &t);
     if (PROBE) return;
     if (c.tile_cnt) cta_tile_count(c.tile_cnt, t);
@@ -1502,6 +1550,7 @@ __device__ __forceinline__ void relax_warp_one(
 // back (a row too long for a mask: the densest, whose one-thread walks were
 // the long tail).  Grid-stride loops: the counts are known on the device
 // only.  Block 0 adds the counts to the fallback statistics.
+template <bool LM = false>
 __global__ void __launch_bounds__(kBlock, 4)
 k_relax_fallback(Ctx c, const float4 *__restrict__ xr, const ulonglong2 *__restrict__ mask01,
                  const unsigned long long *__restrict__ mask2, const int4 *__restrict__ rows,
@@ -1518,9 +1567,9 @@ k_relax_fallback(Ctx c, const float4 *__restrict__ xr, const ulonglong2 *__restr
     const unsigned t0 = blockIdx.x * blockDim.x + threadIdx.x;
     const unsigned nt = gridDim.x * blockDim.x;
     for (unsigned k = t0; k < total; k += nt)
-        relax_update_one<false, false, true>(fb_list[k], c, xr, mask01, mask2, rows, prev, ids,
-                                             start, capped, pos_out, vel_out, kr_out, cnt,
-                                             nullptr);
+        relax_update_one<false, false, true, LM>(fb_list[k], c, xr, mask01, mask2, rows, prev,
+                                                 ids, start, capped, pos_out, vel_out, kr_out,
+                                                 cnt, nullptr);
     // the long-row particles: a warp each when they are few enough for one
     // pass of the grid's warps (the long tail of a step with a few dense
     // spots), else a thread each (many dense particles: a warp each would
@@ -1532,9 +1581,9 @@ k_relax_fallback(Ctx c, const float4 *__restrict__ xr, const ulonglong2 *__restr
                            start, capped, pos_out, vel_out, kr_out, cnt);
     } else {
         for (unsigned k = t0; k < total_long; k += nt)
-            relax_update_one<false, false, true>(fb_list[c.n - 1 - (int)k], c, xr, mask01, mask2,
-                                                 rows, prev, ids, start, capped, pos_out, vel_out,
-                                                 kr_out, cnt, nullptr);
+            relax_update_one<false, false, true, LM>(fb_list[c.n - 1 - (int)k], c, xr, mask01,
+                                                     mask2, rows, prev, ids, start, capped,
+                                                     pos_out, vel_out, kr_out, cnt, nullptr);
     }
 }
 
@@ -1862,7 +1911,9 @@ static void enqueue_density(sph_cuda *h)
     auto kd = h->shape[1].persistent ? k_density_sm<true> : k_density_sm<false>;
     const size_t smem = (size_t)kStagePerThread * h->shape[1].block * sizeof(float2);
 #else
-    auto kd = h->shape[1].persistent ? k_density_t<true> : k_density_t<false>;
+    auto kd = h->shape[1].persistent
+                  ? (h->long_masks ? k_density_t<true, true> : k_density_t<true, false>)
+                  : (h->long_masks ? k_density_t<false, true> : k_density_t<false, false>);
     const size_t smem = 0;
 #endif
     launch_step(kd, gather_grid(h, h->shape[1]), h->shape[1].block, smem, h->stream, make_ctx(h),
@@ -1870,6 +1921,10 @@ static void enqueue_density(sph_cuda *h)
                 (const unsigned *)&st->build_max_occ[SLOT_PREDICTED], h->xr_c, h->mask01_c,
                 h->mask2_c, h->rows_c);
 }
+
+// Whether this build's gathers support long-row hit masks (not with the
+// shared-memory staged forms).
+bool long_masks_supported() { return !(SPH_DENS_SMEM || SPH_RELAX_SMEM); }
 
 // The density pass of a step (the learned step's features start with it).
 int launch_density_pass(sph_cuda *h)
@@ -1908,19 +1963,22 @@ int launch_learned_relax(sph_cuda *h, float2 *probe_out, cudaEvent_t *events)
     L.max_nb = h->learned_thr < 0.0f ? -1 : SPH_LEARNED_MAX_NEIGHBORS;
     const int nb = blocks_for(h->n);
     const unsigned *occ = &st->build_max_occ[SLOT_PREDICTED];
+    const bool lm = h->long_masks;
     if (probe_out) {
-        k_relax_learned<true><<<nb, kBlock, 0, h->stream>>>(
+        (lm ? k_relax_learned<true, true> : k_relax_learned<true, false>)<<<nb, kBlock, 0,
+                                                                          h->stream>>>(
             c, h->xr_c, h->mask01_c, h->mask2_c, h->rows_c, h->prev_c, h->id_c, h->start_c, occ,
             nullptr, nullptr, nullptr, nullptr, nullptr, probe_out, L, st, nullptr);
         return cuda_fail(cudaGetLastError(), "learned relaxation probe");
     }
-    k_relax_learned<false><<<nb, kBlock, 0, h->stream>>>(
+    (lm ? k_relax_learned<false, true> : k_relax_learned<false, false>)<<<nb, kBlock, 0,
+                                                                        h->stream>>>(
         c, h->xr_c, h->mask01_c, h->mask2_c, h->rows_c, h->prev_c, h->id_c, h->start_c, occ,
         &st->build_max_occ[SLOT_RELAXED], h->pos_b, h->vel_b, h->kr_b, h->cnt, nullptr, L, st,
         h->fb_list);
     if (events) cudaEventRecord(events[0], h->stream);
     const int fb_blocks = std::min(nb, 4 * h->num_sms);
-    k_relax_fallback<<<fb_blocks, kBlock, 0, h->stream>>>(
+    (lm ? k_relax_fallback<true> : k_relax_fallback<false>)<<<fb_blocks, kBlock, 0, h->stream>>>(
         c, h->xr_c, h->mask01_c, h->mask2_c, h->rows_c, h->prev_c, h->id_c, h->start_c, occ,
         h->pos_b, h->vel_b, h->kr_b, h->cnt, st, h->fb_list);
     if (events) cudaEventRecord(events[1], h->stream);
@@ -1966,7 +2024,11 @@ int enqueue_step(sph_cuda *h, cudaEvent_t *events, int *nkernels, const tunable_
                                          : k_relax_update_sm<false, false>;
         const size_t smem = (size_t)kStagePerThread * h->shape[2].block * sizeof(float4);
 #else
-        auto kr = h->shape[2].persistent ? k_relax_update<false, true> : k_relax_update<false, false>;
+        auto kr = h->shape[2].persistent
+                      ? (h->long_masks ? k_relax_update<false, true, true>
+                                       : k_relax_update<false, true, false>)
+                      : (h->long_masks ? k_relax_update<false, false, true>
+                                       : k_relax_update<false, false, false>);
         const size_t smem = 0;
 #endif
         launch_step(kr, gather_grid(h, h->shape[2]), h->shape[2].block, smem, h->stream, c,

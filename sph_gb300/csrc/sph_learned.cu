@@ -90,6 +90,7 @@ struct NbRec {
 // particle with a coincident neighbour (r2 <= 2e-12, where the reference
 // nudges) or in an overflowing bucket gets count 65535: it always takes the
 // plain relaxation.  Block 0 resets the step's fallback-list counters.
+template <bool LM>
 __global__ void __maxnreg__(48)
 k_messages(Ctx c, const float4 *__restrict__ xr, const ulonglong2 *__restrict__ mask01,
            const unsigned long long *__restrict__ mask2, const int4 *__restrict__ rows,
@@ -164,6 +165,16 @@ k_messages(Ctx c, const float4 *__restrict__ xr, const ulonglong2 *__restrict__ 
         const unsigned long long mm[3] = {m01.x, m01.y, m2};
 #pragma unroll
         for (int r = 0; r < 3; ++r) walk_mask<NbRec>(mm[r], ra[r], c.n, load, visit);
+    } else if (LM && !capped && rw.w == kRowsMasked2) {
+        // long-row masks: each row's two masks in slot order
+        const int ra[3] = {rw.x, rw.y, rw.z};
+        const unsigned long long mm[3] = {m01.x, m01.y, m2};
+        const unsigned long long *mx = c.maskx + 3 * (size_t)i;
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            walk_mask<NbRec>(mm[r], ra[r], c.n, load, visit);
+            walk_mask<NbRec>(__ldg(mx + r), ra[r] + kMaskRow, c.n, load, visit);
+        }
     } else if (!capped && rw.w == kRowsFull) {
         // a stencil row longer than a hit mask: the whole stencil, in slot
         // order
@@ -988,7 +999,8 @@ int train_loop(LearnedModel *l, int first, int nsamples, int epochs, int batch, 
 int launch_messages(sph_cuda *h, __nv_bfloat16 *feat, unsigned short *nbc)
 {
     if (h->n == 0) return SPH_OK;
-    ml::k_messages<<<nblk(h->n), kBlock, 0, h->stream>>>(
+    (h->long_masks ? ml::k_messages<true> : ml::k_messages<false>)<<<nblk(h->n), kBlock, 0,
+                                                                      h->stream>>>(
         make_ctx(h), h->xr_c, h->mask01_c, h->mask2_c, h->rows_c, h->prev_c, h->start_c,
         &h->d_state->build_max_occ[SLOT_PREDICTED], feat, nbc, &h->d_state->fb_count);
     return cuda_fail(cudaGetLastError(), "messages");

@@ -140,9 +140,10 @@ class Simulation:
         check(lib().sph_cuda_set_scene_params(self._h, int(scene), ctypes.byref(tunables(params))))
 
     def autotune(self, trial_steps: int = 3) -> list:
-        """Picks the fastest launch shape per gather kernel by timing
-        graph-launched steps (advances the simulation by 48 * trial_steps
-        steps); returns the 6 shape ints."""
+        """Picks the fastest launch shape per gather kernel, then long-row
+        hit masks on or off (long_row_masks()), by timing graph-launched
+        steps (advances the simulation by 50 * trial_steps steps); returns
+        the 6 shape ints."""
         out = (ctypes.c_int * 6)()
         check(lib().sph_cuda_autotune(self._h, int(trial_steps), out))
         return list(out)
@@ -155,6 +156,14 @@ class Simulation:
     def set_launch_shapes(self, shapes):
         arr = (ctypes.c_int * 6)(*[int(v) for v in shapes])
         check(lib().sph_cuda_set_launch_shapes(self._h, arr))
+
+    def long_row_masks(self) -> bool:
+        """Whether the density pass records hit masks for stencil rows of
+        65..128 candidates (sph_cuda_set_long_row_masks)."""
+        return bool(lib().sph_cuda_get_long_row_masks(self._h))
+
+    def set_long_row_masks(self, on: bool):
+        check(lib().sph_cuda_set_long_row_masks(self._h, 1 if on else 0))
 
     def step_split(self, before: dict | None, after: dict):
         """One step whose tunables switch after the prediction, where the

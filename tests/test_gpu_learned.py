@@ -184,11 +184,13 @@ def test_fallback_only_is_the_plain_step(cuda_lib):
         assert learned.launches_per_step() == 11
 
 
-def test_fallback_only_is_the_plain_step_in_dense_cells(cuda_lib):
+@pytest.mark.parametrize("long_masks", [False, True])
+def test_fallback_only_is_the_plain_step_in_dense_cells(cuda_lib, long_masks):
     """Cells of 25 particles: stencil rows of ~75 candidates, longer than a
-    stored hit mask, so the plain relaxation searches the whole stencil and
-    the fallback pass walks the rows 64 candidates at a time -- the same
-    neighbours in the same order, bit for bit."""
+    stored hit mask, so the plain relaxation searches the whole stencil (or,
+    with long-row masks, walks two masks per row) and the fallback pass
+    walks the rows 64 candidates at a time -- the same neighbours in the same
+    order, bit for bit; and long-row masks change no bit of the plain step."""
     sc = scenes.dam_break(6400, 80, 64.0, 64.0, seed=77, name="dense", lattice=0.2,
                           x0=0.1, y0=0.1)
     gx = np.floor(sc.x / sc.spacing).astype(np.int64)
@@ -196,15 +198,35 @@ def test_fallback_only_is_the_plain_step_in_dense_cells(cuda_lib):
     assert 3 * np.bincount(gy * sc.size_x + gx).max() > 64
     P = sc.params.as_dict()
     with Simulation.from_scene(sc) as plain, Simulation.from_scene(sc) as learned, \
-            LearnedModel(0, seed=5) as m:
-        plain.step(P, 2)
-        learned.step(P, 2)
+            Simulation.from_scene(sc) as ref, LearnedModel(0, seed=5) as m:
+        for s in (plain, learned):
+            s.set_long_row_masks(long_masks)
+            assert s.long_row_masks() == long_masks
+        for s in (plain, learned, ref):
+            s.step(P, 2)
         learned.set_learned(m, threshold=-1.0)
-        plain.step(P, 4)
-        learned.step(P, 4)
-        a, b = plain.download(), learned.download()
+        for s in (plain, learned, ref):
+            s.step(P, 4)
+        a, b, c = plain.download(), learned.download(), ref.download()
         for f in ("x", "y", "v_x", "v_y", "density", "density_near"):
             assert bits_equal(a[f], b[f]), f
+            assert bits_equal(a[f], c[f]), f
+
+
+def test_long_row_masks_leave_the_features_as_they_are(cuda_lib):
+    """The message walk over two masks per long row visits the same
+    neighbours in the same order as the whole-stencil walk."""
+    sc = scenes.dam_break(6400, 80, 64.0, 64.0, seed=78, name="dense", lattice=0.2,
+                          x0=0.1, y0=0.1)
+    P = sc.params.as_dict()
+    with Simulation.from_scene(sc) as a, Simulation.from_scene(sc) as b:
+        b.set_long_row_masks(True)
+        a.step(P, 3)
+        b.step(P, 3)
+        fa, ca = a.learned_features()
+        fb, cb = b.learned_features()
+    assert np.array_equal(ca, cb)
+    assert bits_equal(fa, fb)
 
 
 def rms_density_error(sc, model, state_steps, threshold):
