@@ -23,11 +23,13 @@ def run_alone(sc, steps):
         return s.download(), s.diagnostics()
 
 
-def run_ensemble(scs, steps, shapes=None, autotune=False):
+def run_ensemble(scs, steps, shapes=None, autotune=False, long_masks=False):
     e = Ensemble(scs)
     e.upload_scenes()
     if shapes is not None:
         e.set_launch_shapes(shapes)
+    if long_masks:
+        e.set_long_row_masks(True)
     if autotune:
         chosen = e.autotune(1)  # advances 48 steps
         # re-upload so every run starts from the same state
@@ -62,6 +64,18 @@ def test_launch_shapes_do_not_change_results(cuda_lib):
     got, _ = run_ensemble(scs, 10, autotune=True)
     for f in ref:
         assert bits_equal(got[f], ref[f]), f
+
+
+def test_long_row_masks_do_not_change_results(cuda_lib):
+    """Dense scenes (cells of ~25 particles: stencil rows of ~75
+    candidates) with and without long-row hit masks: the same bits."""
+    scs = [scenes.dam_break(6400, 80, 64.0, 64.0, seed=90 + s, name=f"dense_{s}", lattice=0.2,
+                            x0=0.1, y0=0.1) for s in range(3)]
+    ref, rd = run_ensemble(scs, 8)
+    got, gd = run_ensemble(scs, 8, long_masks=True)
+    for f in ref:
+        assert bits_equal(got[f], ref[f]), f
+    assert np.array_equal(rd, gd)
 
 
 def test_ensemble_scenes_follow_cpu_jacobi(cuda_lib):
