@@ -73,8 +73,14 @@ constexpr int kScanThreads = 256;
 constexpr int kScanItems = 16;                        // per thread
 constexpr int kScanTile = kScanThreads * kScanItems;  // cells per scan tile
 // tiles of a step's cell build (k_cell_starts), counted by the key producers
-constexpr int kBuildThreads = 256;
-constexpr int kBuildItems = 16;
+#ifndef SPH_BUILD_THREADS
+#define SPH_BUILD_THREADS 256
+#endif
+#ifndef SPH_BUILD_ITEMS
+#define SPH_BUILD_ITEMS 16
+#endif
+constexpr int kBuildThreads = SPH_BUILD_THREADS;  // cell-starts CTA
+constexpr int kBuildItems = SPH_BUILD_ITEMS;      // cell counters per thread
 constexpr int kBuildTile = kBuildThreads * kBuildItems;
 static_assert(kBuildTile >= kScanTile, "the build's tile counts fit the scan tile buffer");
 constexpr int kBlock = 256;                           // default particle-kernel block
